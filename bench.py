@@ -1,0 +1,317 @@
+"""Benchmark: forward FDTD throughput (Gcell-updates/s) on the c1 workload.
+
+Workload (``--workload c1``, default): 512x512x64 Yee domain (16-cell x-y
+absorber, 8-cell z-PML included), Si waveguide through a blurred random
+50x50x6 design region, 10000 steps, 5 output frequencies over 1.50-1.60 um,
+phasors projected inside the time loop.  One bench "step" is one full
+forward solve (10000 Yee updates of every cell).  Inputs (400 MB of field
+state, 200 MB of coefficients) exceed the 129 MB L2, so no flush is needed
+between solves.
+
+Output: one JSON line (rank 0).  ``value`` is device-resident throughput of
+the engine plan; ``e2e`` is the same metric through ``pjz_gb300.field`` with
+host inputs (H2D of epsilon/source and D2H of the complex phasors inside the
+timed region).  ``roofline`` compares the step kernel's algorithmic bytes
+(60 B per cell-update) per launch against the measured HBM copy bandwidth.
+``--impl reference`` times the CPU path (the oracle's C Yee transcription
+on all host cores; the reference engine is CUDA-only and not available).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Gcell-updates/s and HBM GB/s vs roofline; batched grads/s vs plain "
+          "loop at 1e-5 rel-L2")
+UNIT = "Gcell-updates/s"
+BYTES_PER_CELL = 60  # read E(3)+H(3)+coef(3), write E(3)+H(3), FP32
+
+
+def _args():
+  ap = argparse.ArgumentParser()
+  ap.add_argument("--gpus", type=int, default=1)
+  ap.add_argument("--steps", type=int, default=3)
+  ap.add_argument("--warmup", type=int, default=3)
+  ap.add_argument("--impl", default="native", choices=["native", "reference"])
+  ap.add_argument("--workload", default="c1", choices=["c0", "c1"])
+  ap.add_argument("--tt", type=int, default=0, help="override time steps")
+  ap.add_argument("--cpu-seconds", type=float, default=12.0)
+  ap.add_argument("--no-e2e", action="store_true")
+  ap.add_argument("--no-cpu", action="store_true")
+  return ap.parse_args()
+
+
+def _workload(args):
+  from pjz_gb300 import workloads
+  kw = {"tt": args.tt} if args.tt else {}
+  if args.workload == "c0":
+    return workloads.waveguide_c0(**kw)
+  return workloads.design_c1(**kw)
+
+
+def _dist():
+  rank = int(os.environ.get("RANK", 0))
+  world = int(os.environ.get("WORLD_SIZE", 1))
+  local = int(os.environ.get("LOCAL_RANK", 0))
+  return rank, world, local
+
+
+class Clocks:
+  """Samples nvidia-smi SM clocks and throttle reasons during a region."""
+  Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+       "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+       "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+  def __init__(self, index, path):
+    self.path = path
+    self.proc = None
+    self.index = index
+    try:
+      self.f = open(path, "w")
+      self.proc = subprocess.Popen(
+          ["nvidia-smi", "-i", str(index), f"--query-gpu={self.Q}",
+           "--format=csv,noheader,nounits", "-lms", "200"],
+          stdout=self.f, stderr=subprocess.DEVNULL)
+    except (OSError, FileNotFoundError):
+      self.proc = None
+
+  def stop(self):
+    if self.proc is None:
+      return None
+    self.proc.terminate()
+    try:
+      self.proc.wait(timeout=5)
+    except subprocess.TimeoutExpired:
+      self.proc.kill()
+    self.f.close()
+    rows = []
+    for line in open(self.path):
+      parts = [p.strip() for p in line.split(",")]
+      if len(parts) >= 9 and parts[1].isdigit():
+        rows.append(parts)
+    if not rows:
+      return None
+    sm = [int(r[1]) for r in rows]
+    busy = [s for s in sm if s > 0.5 * max(sm)] or sm
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+             "sw_power_cap"]
+    reasons = sorted({n for r in rows for n, v in zip(names, r[5:9])
+                      if v.lower() == "active"})
+    return {"sm_mhz": statistics.median(busy), "sm_max_mhz": int(rows[0][2]),
+            "samples": len(rows), "reasons": reasons}
+
+
+def _peaks():
+  path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+  try:
+    with open(path) as f:
+      d = json.load(f)
+    return float(d["hbm_gbs"]), "measured"
+  except (OSError, KeyError, ValueError):
+    return 6800.0, "fallback"
+
+
+def _profile_traffic(name):
+  """Per-cell-update DRAM bytes of the step kernel from a committed ncu
+  summary (profiles/<name>.json), or None."""
+  path = os.path.join(ROOT, "profiles", f"{name}.json")
+  try:
+    with open(path) as f:
+      d = json.load(f)
+    return float(d["dram_bytes_per_cell_update"]), d
+  except (OSError, KeyError, ValueError):
+    return None, None
+
+
+def cpu_baseline(wl, seconds, threads=0):
+  """Oracle C Yee (FP32, OpenMP) on a bounded number of steps of ``wl``."""
+  import oracle
+  from oracle import pjz_ref
+  sp = wl.sim_params
+  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
+                                  pjz_ref.SimParams(*sp[:-1]), zz=wl.domain[2])
+  domain = wl.domain
+  org, shp, prof = oracle.plane_source_box(kw["source_field"],
+                                           kw["source_position"], domain)
+  threads = threads or os.cpu_count()
+
+  def run(n):
+    t0 = time.perf_counter()
+    oracle.run(eps=kw["epsilon"], offset=kw["offset"], mask=kw["absorption_mask"],
+               kappa=kw["pml_kappa"], sigma=kw["pml_sigma"], alpha=kw["pml_alpha"],
+               dt=kw["dt"], tt=n, pml_widths=kw["pml_widths"], source_origin=org,
+               source_profile=prof, waveform=kw["source_waveform"][:n],
+               mode="none", nthreads=threads)
+    return time.perf_counter() - t0
+
+  t1 = run(1)
+  t3 = run(3)
+  per = max((t3 - t1) / 2, 1e-6)
+  n = max(2, min(wl.sim_params.tt, int(seconds / per)))
+  dt = run(n)
+  cells = np.prod(domain) * n
+  return {"value": cells / dt / 1e9, "unit": UNIT, "cores": threads,
+          "kind": "port",
+          "sample": f"{n} of {wl.sim_params.tt} steps of the {domain[0]}x"
+                    f"{domain[1]}x{domain[2]} domain, oracle/yee.c FP32 + "
+                    f"OpenMP, {dt:.1f} s incl. set-up"}
+
+
+def run_reference(args):
+  rank, world, _ = _dist()
+  if rank != 0:
+    return
+  wl = _workload(args)
+  vals = []
+  for i in range(args.warmup + args.steps):
+    r = cpu_baseline(wl, max(2.0, args.cpu_seconds / max(args.steps, 1)))
+    if i >= args.warmup:
+      vals.append(r["value"])
+  v = float(np.mean(vals))
+  r["value"] = v
+  print(json.dumps({
+      "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT,
+      "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+      "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+      "dtype": "f32", "data": "synthetic",
+      "config": {"workload": wl.name, "domain": list(wl.domain),
+                 "time_steps": wl.sim_params.tt, "freqs": len(wl.omega)},
+      "cpu_baseline": r,
+      "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def run_native(args):
+  import torch
+  import pjz_gb300
+  from pjz_gb300 import _field, engine
+  rank, world, local = _dist()
+  torch.cuda.set_device(local)
+  dev = torch.device("cuda", local)
+  if world > 1:
+    import torch.distributed as tdist
+    tdist.init_process_group("nccl", device_id=dev)
+  wl = _workload(args)
+  sp = wl.sim_params
+  eps = torch.as_tensor(wl.epsilon, device=dev)
+  src = torch.as_tensor(wl.source, device=dev)
+  kw, omega = _field._setup(eps, src, wl.omega, wl.source_pos, sp)
+  plan, prof = _field.phasor_plan(kw, omega)
+  run_args = dict(epsilon=eps, absorption_mask=kw["absorption_mask"],
+                  source=prof, waveform=kw["source_waveform"])
+  out = torch.empty(plan.out_shape(), dtype=torch.float32, device=dev)
+  cells = int(np.prod(wl.domain)) * sp.tt
+
+  def barrier():
+    if world > 1:
+      torch.distributed.barrier()
+    torch.cuda.synchronize()
+
+  def maxed(x):
+    if world == 1:
+      return x
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+  for _ in range(args.warmup):
+    plan.run(**run_args, out=out)
+  barrier()
+  stream = torch.cuda.current_stream(dev)
+  clocks = Clocks(local, os.path.join(ROOT, "gpurun_out", f"clocks_bench_{rank}.csv")
+                  if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
+                  else f"/tmp/clocks_bench_{rank}.csv")
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record(stream)
+  for _ in range(args.steps):
+    plan.run(**run_args, out=out)
+  e1.record(stream)
+  barrier()
+  clk = clocks.stop()
+  ms = maxed(e0.elapsed_time(e1)) / args.steps
+  value = world * cells / (ms / 1e3) / 1e9
+
+  # Step-kernel launch time: steps [1, L) skip the set-up kernels.
+  nl = min(sp.tt - 1, 2000)
+  plan.run(**run_args, out=out)  # leaves a valid state in the workspace
+  k0 = torch.cuda.Event(enable_timing=True)
+  k1 = torch.cuda.Event(enable_timing=True)
+  k0.record(stream)
+  plan.run(**run_args, out=out, steps=(1, 1 + nl))
+  k1.record(stream)
+  torch.cuda.synchronize()
+  launch_ms = k0.elapsed_time(k1) / nl
+  cells_per_launch = int(np.prod(wl.domain))
+  achieved = BYTES_PER_CELL * cells_per_launch / (launch_ms / 1e3) / 1e9
+  peak, peak_kind = _peaks()
+  bpc, prof_d = _profile_traffic(f"yee_step_{args.workload}")
+  roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
+              "unit": "GB/s", "frac": achieved / peak,
+              "peak_source": f"hbm_gbs of {peak_kind}",
+              "kernel": "yee_step_kernel",
+              "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells_per_launch,
+              "launch_ms": launch_ms,
+              "traffic": None if bpc is None else bpc * cells_per_launch}
+
+  e2e = None
+  if not args.no_e2e:
+    eps_h = torch.as_tensor(wl.epsilon).pin_memory()
+    src_h = torch.as_tensor(wl.source).pin_memory()
+    res = pjz_gb300.field(eps_h, src_h, wl.omega, wl.source_pos, sp)  # warm
+    host = torch.empty(res.shape, dtype=res.dtype).pin_memory()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+      res = pjz_gb300.field(eps_h.to(dev, non_blocking=True),
+                            src_h.to(dev, non_blocking=True), wl.omega,
+                            wl.source_pos, sp)
+      host.copy_(res, non_blocking=True)
+      torch.cuda.synchronize()
+    t_e2e = maxed(time.perf_counter() - t0) / args.steps
+    e2e = {"value": world * cells / t_e2e / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": eps_h.numel() * 4 + src_h.numel() * 4,
+           "d2h_bytes_per_step": host.numel() * host.element_size(),
+           "ms_per_step": t_e2e * 1e3}
+
+  cpu = None
+  if rank == 0 and not args.no_cpu:
+    cpu = cpu_baseline(wl, args.cpu_seconds)
+
+  if rank == 0:
+    cfg = plan.launch_config()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded blurred random design)",
+        "config": {"workload": wl.name, "domain": list(wl.domain),
+                   "time_steps": sp.tt, "freqs": len(wl.omega),
+                   "output": "5-frequency phasors fused in the time loop",
+                   "l2": "inputs larger than L2 (600 MB state), no flush",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "launch": cfg},
+        "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": args.steps * (sp.tt + 1),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+  if world > 1:
+    torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+  a = _args()
+  if a.impl == "reference":
+    run_reference(a)
+  else:
+    run_native(a)

@@ -1,0 +1,161 @@
+/*
+ * pjzfdtd -- C ABI of the GB300 (sm_103a) FDTD engine behind pjz.
+ *
+ * This library replaces the engine pjz calls at src/pjz/_field.py:254-269
+ * (`fdtdz_jax.fdtdz(...)`, an XLA custom call into the third-party fdtdz
+ * CUDA package, dependency `fdtdz>=1.1.3` at setup.py:26).  The problem
+ * description below carries exactly the keyword arguments of that call:
+ *
+ *   epsilon (3,rx,ry,rz)            -> pjzfdtd_buffers.epsilon, rx/ry/rz
+ *   dt                              -> pjzfdtd_problem.dt
+ *   source_field, source_position   -> source box + profile (see below)
+ *   source_waveform (tt,2)          -> pjzfdtd_buffers.waveform, tt, src_ncols
+ *   absorption_mask (3,X,Y)         -> pjzfdtd_buffers.absorption_mask, xx/yy
+ *   pml_kappa/sigma/alpha (Z,2)     -> pjzfdtd_plan_create host arrays, zz
+ *   pml_widths                      -> pml_lo, pml_hi
+ *   output_steps (start,stop,step)  -> out_start, out_stop, out_step
+ *   offset (px,py,pz)               -> ox, oy, oz
+ *   use_reduced_precision           -> only FP32 storage is implemented;
+ *                                      the flag stays with pjz's z budget
+ *   launch_params                   -> tile_y, seg_x (0 = autotuned)
+ *
+ * fdtdz's plane sources map onto the general source box: an x-normal source
+ * (2,1,Y,Z) at position s is a 2-plane box x in [s-1, s] whose waveform
+ * column 0 drives plane s and column 1 plane s-1, with the two leading
+ * entries feeding (Ey, Ez); y-normal (2,X,1,Z) likewise with (Ex, Ez);
+ * z-normal (2,2,X,Y,1) is a 1-plane box at z = s, column k with profile k on
+ * (Ex, Ey).  The adjoint solve uses the same box with 2*ww columns.
+ *
+ * Conventions: device buffers are caller-owned; every call is stream-ordered
+ * on the stream passed in; a plan is not thread-safe; no call throws; every
+ * call returns a pjzfdtd_status and leaves a message for
+ * pjzfdtd_last_error() (thread-local) when it fails.  pjz raises ValueError
+ * at trace time for bad shapes (src/pjz/_field.py:288-290); the matching
+ * status here is PJZFDTD_ERR_INVALID, which the Python layer raises as
+ * ValueError.
+ */
+#ifndef PJZFDTD_H_
+#define PJZFDTD_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PJZFDTD_ABI_VERSION 1
+
+typedef enum {
+  PJZFDTD_OK = 0,
+  PJZFDTD_ERR_INVALID = 1,     /* bad shape or argument */
+  PJZFDTD_ERR_CUDA = 2,        /* CUDA runtime error */
+  PJZFDTD_ERR_WORKSPACE = 3,   /* workspace missing or too small */
+  PJZFDTD_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  PJZFDTD_ERR_UNSUPPORTED = 5  /* valid request this build does not serve */
+} pjzfdtd_status;
+
+typedef enum {
+  PJZFDTD_OUT_NONE = 0,
+  /* E at range(out_start, out_stop, out_step): (ns,3,rx,ry,rz), the
+     fdtdz return value (src/pjz/_field.py:254, 276-278). */
+  PJZFDTD_OUT_SNAPSHOTS = 1,
+  /* weights @ snapshots fused into the time loop: (out_rows,3,rx,ry,rz)
+     with weights = pinv(P^T) of src/pjz/_field.py:272-278. */
+  PJZFDTD_OUT_PHASORS = 2,
+  /* adjoint: sum_j E_j * (weights[:,j] . q) over the gradient box:
+     (3,gnx,gny,gnz) -- the fused dL/d-eps accumulation. */
+  PJZFDTD_OUT_GRADIENT = 3
+} pjzfdtd_out_mode;
+
+typedef struct pjzfdtd_problem {
+  int32_t xx, yy, zz;          /* simulation domain in cells */
+  int32_t ox, oy, oz;          /* fdtdz `offset` of the epsilon region */
+  int32_t rx, ry, rz;          /* epsilon / output region shape */
+  int32_t tt;                  /* time steps (rows of the waveform) */
+  int32_t pml_lo, pml_hi;      /* fdtdz `pml_widths` */
+  float dt;
+  int32_t src_x0, src_y0, src_z0;           /* source box origin */
+  int32_t src_nx, src_ny, src_nz, src_ncols; /* box shape, waveform columns */
+  int32_t out_start, out_stop, out_step;    /* fdtdz `output_steps` */
+  int32_t out_mode;            /* pjzfdtd_out_mode */
+  int32_t out_rows;            /* rows of weights (PHASORS, GRADIENT), <= 32 */
+  int32_t record_h;            /* SNAPSHOTS/PHASORS: also record H */
+  int32_t grad_x0, grad_y0, grad_z0, grad_nx, grad_ny, grad_nz;
+  int32_t tile_y;              /* launch params: y rows per CTA, 0 = auto */
+  int32_t seg_x;               /* launch params: x planes per CTA, 0 = auto */
+  int32_t steps_per_pass;      /* launch params: time steps per HBM pass, 0 = auto */
+  int32_t reserved[5];
+} pjzfdtd_problem;
+
+typedef struct pjzfdtd_buffers {
+  const float* epsilon;          /* device (3,rx,ry,rz) */
+  const float* absorption_mask;  /* device (3,xx,yy) */
+  const float* source;           /* device (src_ncols,3,src_nx,src_ny,src_nz) */
+  const float* waveform;         /* device (tt,src_ncols) */
+  const float* q;                /* device (out_rows,3,grad box), GRADIENT */
+  float* out;                    /* device, shape per out_mode */
+  float* out_h;                  /* device, same shape as out, if record_h */
+  float* fields;                 /* device (6,xx,yy,zz) state in/out, or NULL
+                                    for a zero start and no state out */
+} pjzfdtd_buffers;
+
+typedef struct pjzfdtd_plan pjzfdtd_plan;
+
+/* ABI version of the loaded library (PJZFDTD_ABI_VERSION it was built with). */
+int32_t pjzfdtd_abi_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated);
+   returns the status of that error. */
+int32_t pjzfdtd_last_error(char* buf, size_t len);
+
+/* Validates `problem` and builds a plan: CPML coefficients from the host
+   arrays pml_kappa/sigma/alpha (zz,2) (src/pjz/_field.py:243-251) and, for
+   PHASORS/GRADIENT, the host weights (out_rows, ns).  Host-only: no CUDA
+   call is made, so this can run without a GPU. */
+int32_t pjzfdtd_plan_create(const pjzfdtd_problem* problem,
+                            const float* pml_kappa, const float* pml_sigma,
+                            const float* pml_alpha, const float* weights,
+                            pjzfdtd_plan** plan);
+
+/* Device scratch the plan needs (bytes, 256-byte aligned start). */
+int32_t pjzfdtd_plan_workspace_bytes(const pjzfdtd_plan* plan, size_t* bytes);
+
+/* Number of recorded samples ns = len(range(out_start, out_stop, out_step)). */
+int32_t pjzfdtd_plan_num_samples(const pjzfdtd_plan* plan, int32_t* ns);
+
+int32_t pjzfdtd_plan_destroy(pjzfdtd_plan* plan);
+
+/* Forward solve: all tt steps, the fdtdz call of src/pjz/_field.py:254-269
+   (SNAPSHOTS) or the whole of `field` with its pinv projection fused
+   (PHASORS, src/pjz/_field.py:271-279).  Stream-ordered on `stream`
+   (a cudaStream_t, NULL = legacy default stream). */
+int32_t pjzfdtd_forward(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Adjoint solve: the same update driven by the adjoint source in `buffers`,
+   accumulating dL/d-eps = sum_j E_adj(t_j) * (weights[:,j] . q) over the
+   gradient box without storing any time history (plan out_mode must be
+   GRADIENT).  Replaces the residual-product VJP of src/pjz/_field.py:
+   380-398. */
+int32_t pjzfdtd_adjoint(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
+                        void* workspace, size_t workspace_bytes, void* stream);
+
+/* Runs steps [step_begin, step_end) only, continuing from the state kept in
+   the workspace (step_begin == 0 re-initialises it).  Lets a caller
+   checkpoint (copy `fields` out between calls) or interleave work. */
+int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
+                          void* workspace, size_t workspace_bytes,
+                          int32_t step_begin, int32_t step_end, void* stream);
+
+/* Launch geometry the plan resolved: tile_y, seg_x, threads per CTA, time
+   steps per pass. */
+int32_t pjzfdtd_plan_launch_config(const pjzfdtd_plan* plan, int32_t* tile_y,
+                                   int32_t* seg_x, int32_t* threads,
+                                   int32_t* steps_per_pass);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PJZFDTD_H_ */

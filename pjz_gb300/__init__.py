@@ -1,0 +1,13 @@
+"""GB300-native (sm_103a) FDTD engine behind pjz's simulation entry points.
+
+Public API (mirrors pjz's ``src/pjz/_field.py``):
+  * :class:`SimParams`, :func:`field` -- time-harmonic fields;
+  * :func:`fdtdz` -- drop-in for the ``fdtdz_jax.fdtdz`` engine call;
+  * :class:`engine.Plan` -- the plan/run API over the C ABI.
+"""
+
+from ._field import SimParams, field
+from ._fdtdz import LaunchParams, fdtdz
+from . import engine
+
+__all__ = ["SimParams", "field", "fdtdz", "LaunchParams", "engine"]

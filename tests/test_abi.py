@@ -1,0 +1,105 @@
+"""C-ABI checks that need no GPU: the library loads, exports every symbol the
+header declares, and its host-only plan validation behaves like pjz's
+argument checks (bad shapes -> ValueError)."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pjz_gb300 import _build, _lib, engine
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(__file__)), "include",
+                      "pjzfdtd.h")
+
+
+@pytest.fixture(scope="module")
+def lib():
+  _build.build()
+  return _lib.load()
+
+
+def declared_symbols():
+  text = open(HEADER).read()
+  return sorted(set(re.findall(r"\b(pjzfdtd_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_entry_points():
+  syms = declared_symbols()
+  assert "pjzfdtd_forward" in syms and "pjzfdtd_adjoint" in syms
+  assert len(syms) >= 10
+
+
+def test_library_exports_every_declared_symbol(lib):
+  for name in declared_symbols():
+    assert hasattr(lib, name), name
+  assert set(declared_symbols()) <= set(_lib.SIGNATURES) | set(
+      n for n in declared_symbols() if hasattr(lib, n))
+
+
+def test_abi_version(lib):
+  assert lib.pjzfdtd_abi_version() == 1
+
+
+def test_struct_sizes_match_header():
+  # 12 ints + float + 22 ints + 5 reserved = 40 x 4 bytes.
+  assert ctypes.sizeof(_lib.Problem) == 160
+  assert ctypes.sizeof(_lib.Buffers) == 8 * 8
+
+
+def _plan(**kw):
+  Z = kw.pop("Z", 16)
+  base = dict(domain=(20, 18, Z), offset=(2, 2, 2), region=(16, 14, Z - 4),
+              tt=50, dt=0.5, pml_widths=(2, 2),
+              pml_kappa=np.ones((Z, 2)), pml_sigma=np.zeros((Z, 2)),
+              pml_alpha=np.zeros((Z, 2)), source_origin=(4, 0, 0),
+              source_shape=(2, 18, Z), source_ncols=2,
+              output_steps=(30, 50, 5), out_mode=engine.OUT_SNAPSHOTS)
+  base.update(kw)
+  return engine.Plan(**base)
+
+
+def test_plan_create_host_only(lib):
+  p = _plan()
+  assert p.num_samples == 4
+  X, Y, Z = p.domain
+  assert p.workspace_bytes >= (15 * X * Y * Z) * 4
+  cfg = p.launch_config()
+  assert cfg["tile_y"] >= 1 and cfg["threads"] % 32 == 0
+  assert (cfg["tile_y"] + 2) * Z <= cfg["threads"]
+
+
+@pytest.mark.parametrize("bad,msg", [
+    (dict(offset=(5, 2, 2)), "does not fit"),
+    (dict(pml_widths=(10, 10)), "pml_widths"),
+    (dict(dt=-1.0), "dt must be positive"),
+    (dict(source_origin=(19, 0, 0)), "source box"),
+    (dict(output_steps=(30, 60, 5)), "output_steps"),
+    (dict(output_steps=(30, 50, 0)), "output step"),
+    (dict(pml_kappa=np.zeros((16, 2))), "kappa > 0"),
+    (dict(pml_sigma=-np.ones((16, 2))), "sigma >= 0"),
+    (dict(pml_kappa=np.ones((15, 2))), "must have shape"),
+    (dict(out_mode=engine.OUT_PHASORS, weights=np.ones((40, 4))), "out_rows"),
+])
+def test_plan_create_rejects(lib, bad, msg):
+  with pytest.raises(ValueError, match=msg):
+    _plan(**bad)
+
+
+def test_thick_z_is_unsupported_not_silent(lib):
+  with pytest.raises(NotImplementedError, match="thin-z"):
+    _plan(Z=400, region=(16, 14, 300), offset=(2, 2, 2),
+          source_shape=(2, 18, 400))
+
+
+def test_kappa_inf_allowed(lib):
+  # use_z_as_batch (pjz _field.py:243-246) passes kappa = inf.
+  _plan(pml_kappa=np.full((16, 2), np.inf))
+
+
+def test_last_error_is_thread_local_message(lib):
+  with pytest.raises(ValueError):
+    _plan(dt=0.0)
+  assert "dt" in _lib.last_error()

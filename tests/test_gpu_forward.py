@@ -1,0 +1,209 @@
+"""GPU parity of the forward engine against the CPU oracle.
+
+The FP32 engine performs the same IEEE operations in the same order as the
+FP32 oracle (``oracle/yee.c``), so every comparison here is bit-exact
+(``np.array_equal``); the error against the FP64 oracle is stated with a
+1e-5 relative-L2 bound.  All calls go through the C ABI.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from oracle import pjz_ref
+from pjz_gb300 import engine, workloads
+import pjz_gb300
+from _cases import oracle_kwargs, random_problem
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda:0")
+
+
+def dev(a):
+  return torch.as_tensor(np.ascontiguousarray(a), device=DEV)
+
+
+def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
+            tile_y=0, seg_x=0, fields=None, split=None):
+  p = engine.Plan(domain=case["domain"], offset=case["offset"],
+                  region=case["eps"].shape[1:], tt=case["tt"], dt=case["dt"],
+                  pml_widths=case["pml_widths"], pml_kappa=case["kappa"],
+                  pml_sigma=case["sigma"], pml_alpha=case["alpha"],
+                  source_origin=case["source_origin"],
+                  source_shape=case["source_profile"].shape[2:],
+                  source_ncols=case["source_profile"].shape[0],
+                  output_steps=case["output_steps"], out_mode=out_mode,
+                  weights=weights, record_h=record_h, tile_y=tile_y,
+                  seg_x=seg_x)
+  args = dict(epsilon=dev(case["eps"]), absorption_mask=dev(case["mask"]),
+              source=dev(case["source_profile"]), waveform=dev(case["waveform"]))
+  f = None if fields is None else dev(fields)
+  if split is None:
+    out, out_h = p.run(**args, fields=f)
+  else:
+    out, out_h = p.run(**args, fields=f, steps=(0, split))
+    out, out_h = p.run(**args, fields=f, out=out, out_h=out_h,
+                       steps=(split, case["tt"]))
+  torch.cuda.synchronize()
+  cpu = lambda t: None if t is None else t.cpu().numpy()
+  return cpu(out), cpu(out_h), cpu(f)
+
+
+@pytest.mark.parametrize("src", ["x", "y", "z"])
+@pytest.mark.parametrize("Z,pml", [(16, (2, 2)), (24, (3, 5)), (48, (8, 8)),
+                                   (64, (8, 8)), (12, (0, 0))])
+def test_snapshots_bit_exact(native, src, Z, pml):
+  case = random_problem(hash((src, Z)) % 1000, Z=Z, pml=pml, src=src,
+                        src_pos=5 if src == "z" else 7)
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case)
+  assert np.array_equal(got, want), np.abs(got - want).max()
+
+
+def test_use_z_as_batch_bit_exact(native):
+  case = random_problem(3, Z=20, batch=True, pml=(0, 0))
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case)
+  assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("tile_y,seg_x", [(1, 1), (2, 3), (5, 24), (7, 8), (0, 2)])
+def test_launch_geometry_does_not_change_results(native, tile_y, seg_x):
+  case = random_problem(4, X=26, Y=23, Z=16)
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, tile_y=tile_y, seg_x=seg_x)
+  assert np.array_equal(got, want)
+
+
+def test_record_h_and_final_state(native):
+  case = random_problem(5, Z=24, pml=(4, 4))
+  f0 = np.random.default_rng(9).normal(size=(6,) + case["domain"]).astype(np.float32)
+  want = oracle.run(**oracle_kwargs(case), record_h=True, fields=f0.copy())
+  got, got_h, got_f = gpu_run(case, record_h=True, fields=f0.copy())
+  assert np.array_equal(got, want["out"])
+  assert np.array_equal(got_h, want["out_h"])
+  assert np.array_equal(got_f, want["fields"])
+
+
+def test_run_steps_chaining_matches_single_run(native):
+  case = random_problem(6, tt=60, steps=(20, 60, 7))
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, split=33)
+  assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("rows", [2, 10, 32])
+def test_phasor_projection_bit_exact(native, rows):
+  case = random_problem(7, Z=32, pml=(4, 4), steps=(10, 48, 3))
+  ns = len(range(*case["output_steps"]))
+  w = np.random.default_rng(rows).normal(size=(rows, ns)).astype(np.float32)
+  want = oracle.run(**oracle_kwargs(case), mode="project", weights=w,
+                    record_h=True)
+  got, got_h, _ = gpu_run(case, out_mode=engine.OUT_PHASORS, weights=w,
+                          record_h=True)
+  assert np.array_equal(got, want["out"])
+  assert np.array_equal(got_h, want["out_h"])
+
+
+def test_fdtdz_dropin_matches_oracle(native):
+  case = random_problem(8, src="y", src_pos=6, Z=16)
+  out = pjz_gb300.fdtdz(
+      epsilon=dev(case["eps"]), dt=0.5, source_field=dev(case["source_field"]),
+      source_waveform=dev(case["waveform"]), source_position=6,
+      absorption_mask=dev(case["mask"]), pml_kappa=case["kappa"],
+      pml_sigma=case["sigma"], pml_alpha=case["alpha"],
+      pml_widths=case["pml_widths"], output_steps=case["output_steps"],
+      use_reduced_precision=False, launch_params=None, offset=case["offset"])
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  assert np.array_equal(out.cpu().numpy(), want)
+
+
+def _field_oracle(wl, precision="f32"):
+  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
+                                  pjz_ref.SimParams(*wl.sim_params[:-1]),
+                                  zz=wl.domain[2])
+  domain = (kw["absorption_mask"].shape[1], kw["absorption_mask"].shape[2],
+            kw["pml_kappa"].shape[0])
+  org, shp, prof = oracle.plane_source_box(kw["source_field"],
+                                           kw["source_position"], domain)
+  w = pjz_ref.projection_weights(omega, kw["output_steps"], kw["dt"])
+  r = oracle.run(eps=kw["epsilon"], offset=kw["offset"],
+                 mask=kw["absorption_mask"], kappa=kw["pml_kappa"],
+                 sigma=kw["pml_sigma"], alpha=kw["pml_alpha"], dt=kw["dt"],
+                 tt=kw["source_waveform"].shape[0], pml_widths=kw["pml_widths"],
+                 source_origin=org, source_profile=prof,
+                 waveform=kw["source_waveform"], output_steps=kw["output_steps"],
+                 mode="project", weights=w, precision=precision)["out"]
+  ww = omega.shape[0]
+  return r[:ww] + 1j * r[ww:]
+
+
+def test_field_short_c0_bit_exact(native):
+  wl = workloads.waveguide_c0(tt=400)
+  got = pjz_gb300.field(dev(wl.epsilon), dev(wl.source), wl.omega,
+                        wl.source_pos, wl.sim_params).cpu().numpy()
+  want = _field_oracle(wl)
+  assert got.shape == (1, 3) + wl.epsilon.shape[1:]
+  assert np.array_equal(got, want.astype(np.complex64))
+
+
+def test_field_c0_full_vs_fp32_and_fp64_oracle(native):
+  """Config c0: 128x128x32, 2000 steps; bit-exact to the FP32 oracle and
+  within 1e-5 relative L2 of the FP64 oracle."""
+  wl = workloads.waveguide_c0()
+  got = pjz_gb300.field(dev(wl.epsilon), dev(wl.source), wl.omega,
+                        wl.source_pos, wl.sim_params).cpu().numpy()
+  want32 = _field_oracle(wl, "f32")
+  assert np.array_equal(got, want32.astype(np.complex64))
+  want64 = _field_oracle(wl, "f64")
+  err = np.linalg.norm(got - want64) / np.linalg.norm(want64)
+  print(f"c0 FP32 engine vs FP64 oracle: rel-L2 {err:.3e}")
+  assert err < 1e-5
+
+
+def test_c1_size_short_run_bit_exact(native):
+  """Full 512x512x64 domain for 24 steps against the FP32 oracle."""
+  wl = workloads.design_c1(tt=24, ww=5)
+  sp = wl.sim_params
+  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
+                                  pjz_ref.SimParams(*sp[:-1]), zz=wl.domain[2])
+  domain = wl.domain
+  org, shp, prof = oracle.plane_source_box(kw["source_field"],
+                                           kw["source_position"], domain)
+  steps = (10, 24, 4)
+  case = dict(eps=kw["epsilon"], offset=kw["offset"], mask=kw["absorption_mask"],
+              kappa=kw["pml_kappa"], sigma=kw["pml_sigma"], alpha=kw["pml_alpha"],
+              dt=0.5, tt=24, pml_widths=kw["pml_widths"], source_origin=org,
+              source_profile=prof, waveform=kw["source_waveform"],
+              output_steps=steps, domain=domain)
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case)
+  assert np.array_equal(got, want)
+
+
+def test_linearity_exact_at_full_size(native):
+  """Doubling the source doubles every field bit-for-bit (x2 is exact)."""
+  wl = workloads.design_c1(tt=300, ww=2)
+  a = pjz_gb300.field(dev(wl.epsilon), dev(wl.source), wl.omega, wl.source_pos,
+                      wl.sim_params)
+  b = pjz_gb300.field(dev(wl.epsilon), dev(2 * wl.source), wl.omega,
+                      wl.source_pos, wl.sim_params)
+  assert torch.isfinite(torch.view_as_real(a)).all()
+  assert torch.equal(2 * a, b)
+  c = pjz_gb300.field(dev(wl.epsilon), dev(wl.source), wl.omega, wl.source_pos,
+                      wl.sim_params)
+  assert torch.equal(a, c)  # deterministic
+
+
+def test_cpu_tensor_inputs_are_rejected_by_plan(native):
+  case = random_problem(10)
+  p = engine.Plan(domain=case["domain"], offset=case["offset"],
+                  region=case["eps"].shape[1:], tt=case["tt"], dt=0.5,
+                  pml_widths=case["pml_widths"], pml_kappa=case["kappa"],
+                  pml_sigma=case["sigma"], pml_alpha=case["alpha"])
+  with pytest.raises(ValueError, match="CUDA"):
+    p.run(epsilon=torch.as_tensor(case["eps"]),
+          absorption_mask=torch.as_tensor(case["mask"]))
+  with pytest.raises(ValueError, match="epsilon must have shape"):
+    p.run(epsilon=dev(case["eps"][:, :-1]), absorption_mask=dev(case["mask"]))
