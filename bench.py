@@ -47,6 +47,11 @@ def _args():
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--no-e2e", action="store_true")
   ap.add_argument("--no-cpu", action="store_true")
+  ap.add_argument("--kernel", type=int, default=0,
+                  help="0 auto, 1 register-marching, 2 streamed")
+  ap.add_argument("--stages", type=int, default=0)
+  ap.add_argument("--tile-y", type=int, default=0)
+  ap.add_argument("--seg-x", type=int, default=0)
   return ap.parse_args()
 
 
@@ -54,8 +59,13 @@ def _workload(args):
   from pjz_gb300 import workloads
   kw = {"tt": args.tt} if args.tt else {}
   if args.workload == "c0":
-    return workloads.waveguide_c0(**kw)
-  return workloads.design_c1(**kw)
+    wl = workloads.waveguide_c0(**kw)
+  else:
+    wl = workloads.design_c1(**kw)
+  lp = wl.sim_params.launch_params._replace(
+      kernel=getattr(args, "kernel", 0), stages=getattr(args, "stages", 0),
+      tile_y=getattr(args, "tile_y", 0), seg_x=getattr(args, "seg_x", 0))
+  return wl._replace(sim_params=wl.sim_params._replace(launch_params=lp))
 
 
 def _dist():

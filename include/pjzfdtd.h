@@ -85,7 +85,10 @@ typedef struct pjzfdtd_problem {
   int32_t tile_y;              /* launch params: y rows per CTA, 0 = auto */
   int32_t seg_x;               /* launch params: x planes per CTA, 0 = auto */
   int32_t steps_per_pass;      /* launch params: time steps per HBM pass, 0 = auto */
-  int32_t reserved[5];
+  int32_t kernel;              /* launch params: 0 auto, 1 register-marching,
+                                  2 bulk-copy streamed (needs zz % 4 == 0) */
+  int32_t stages;              /* launch params: streamed ring depth, 0 = auto */
+  int32_t reserved[3];
 } pjzfdtd_problem;
 
 typedef struct pjzfdtd_buffers {
@@ -148,11 +151,19 @@ int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
                           void* workspace, size_t workspace_bytes,
                           int32_t step_begin, int32_t step_end, void* stream);
 
-/* Launch geometry the plan resolved: tile_y, seg_x, threads per CTA, time
-   steps per pass. */
+/* Reads (and clears) the device status word of `workspace` after the work
+   queued on `stream` so far: PJZFDTD_ERR_TIMEOUT if a bounded device-side
+   wait gave up, PJZFDTD_OK otherwise.  Synchronises `stream`. */
+int32_t pjzfdtd_plan_status(pjzfdtd_plan* plan, void* workspace,
+                            size_t workspace_bytes, void* stream);
+
+/* Launch geometry the plan resolved: tile_y, seg_x (0 until the first run
+   picks it for the device), threads per CTA, time steps per pass, kernel
+   variant (1 register-marching, 2 streamed) and streamed ring depth. */
 int32_t pjzfdtd_plan_launch_config(const pjzfdtd_plan* plan, int32_t* tile_y,
                                    int32_t* seg_x, int32_t* threads,
-                                   int32_t* steps_per_pass);
+                                   int32_t* steps_per_pass, int32_t* kernel,
+                                   int32_t* stages);
 
 #ifdef __cplusplus
 }

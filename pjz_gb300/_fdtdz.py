@@ -25,6 +25,8 @@ class LaunchParams(NamedTuple):
   seg_x: int = 0
   steps_per_pass: int = 0
   zz: int = 0
+  kernel: int = 0
+  stages: int = 0
 
 
 def launch_knobs(launch_params: Any) -> LaunchParams:
@@ -113,14 +115,15 @@ def fdtdz(
   region = tuple(int(v) for v in eps.shape[1:])
   key = ("fdtdz", domain, region, tuple(offset), tt, float(dt), origin, shape,
          steps, tuple(pml_widths), _key_array(pml_kappa), _key_array(pml_sigma),
-         _key_array(pml_alpha), knobs[:3])
+         _key_array(pml_alpha), knobs)
   plan = cached_plan(key, lambda: engine.Plan(
       domain=domain, offset=offset, region=region, tt=tt, dt=dt,
       pml_widths=pml_widths, pml_kappa=pml_kappa, pml_sigma=pml_sigma,
       pml_alpha=pml_alpha, source_origin=origin, source_shape=shape,
       source_ncols=2, output_steps=steps, out_mode=engine.OUT_SNAPSHOTS,
       tile_y=knobs.tile_y, seg_x=knobs.seg_x,
-      steps_per_pass=knobs.steps_per_pass))
+      steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
+      stages=knobs.stages))
   out, _ = plan.run(epsilon=eps, absorption_mask=mask, source=prof,
                     waveform=wave)
   return out

@@ -248,7 +248,7 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
          shape, kw["output_steps"], kw["pml_widths"],
          _key_array(kw["pml_kappa"]), _key_array(kw["pml_sigma"]),
          _key_array(kw["pml_alpha"]), weights.tobytes(), bool(record_h),
-         knobs[:3])
+         knobs)
   plan = cached_plan(key, lambda: engine.Plan(
       domain=domain, offset=kw["offset"], region=region, tt=tt, dt=kw["dt"],
       pml_widths=kw["pml_widths"], pml_kappa=kw["pml_kappa"],
@@ -256,7 +256,8 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
       source_origin=origin, source_shape=shape, source_ncols=2,
       output_steps=kw["output_steps"], out_mode=out_mode, weights=weights,
       record_h=record_h, tile_y=knobs.tile_y, seg_x=knobs.seg_x,
-      steps_per_pass=knobs.steps_per_pass))
+      steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
+      stages=knobs.stages))
   return plan, prof
 
 

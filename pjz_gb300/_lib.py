@@ -20,7 +20,7 @@ _PROBLEM_INTS2 = (
     "src_x0", "src_y0", "src_z0", "src_nx", "src_ny", "src_nz", "src_ncols",
     "out_start", "out_stop", "out_step", "out_mode", "out_rows", "record_h",
     "grad_x0", "grad_y0", "grad_z0", "grad_nx", "grad_ny", "grad_nz",
-    "tile_y", "seg_x", "steps_per_pass")
+    "tile_y", "seg_x", "steps_per_pass", "kernel", "stages")
 
 
 class Problem(ctypes.Structure):
@@ -28,7 +28,7 @@ class Problem(ctypes.Structure):
   _fields_ = ([(n, ctypes.c_int32) for n in _PROBLEM_INTS]
               + [("dt", ctypes.c_float)]
               + [(n, ctypes.c_int32) for n in _PROBLEM_INTS2]
-              + [("reserved", ctypes.c_int32 * 5)])
+              + [("reserved", ctypes.c_int32 * 3)])
 
 
 class Buffers(ctypes.Structure):
@@ -55,9 +55,8 @@ SIGNATURES = {
                              _P]),
     "pjzfdtd_run_steps": (_I, [_P, ctypes.POINTER(Buffers), _P,
                                ctypes.c_size_t, _I, _I, _P]),
-    "pjzfdtd_plan_launch_config": (_I, [_P, ctypes.POINTER(_I),
-                                        ctypes.POINTER(_I), ctypes.POINTER(_I),
-                                        ctypes.POINTER(_I)]),
+    "pjzfdtd_plan_launch_config": (_I, [_P] + [ctypes.POINTER(_I)] * 6),
+    "pjzfdtd_plan_status": (_I, [_P, _P, ctypes.c_size_t, _P]),
 }
 
 _lib = None

@@ -16,6 +16,7 @@
 
 #include "../../include/pjzfdtd.h"
 #include "step_kernel.cuh"
+#include "stream_kernel.cuh"
 
 using namespace pjzfdtd;
 
@@ -53,9 +54,12 @@ struct pjzfdtd_plan {
   std::vector<float> weights;  // [rows][ns]
   // Resolved launch geometry.
   int tile_y = 0, seg_x = 0, threads = 0, steps_per_pass = 1;
+  int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed
+  int stages = 0;   // streamed ring depth
+  size_t smem = 0;  // dynamic shared memory per CTA
   // Workspace layout (byte offsets).
   size_t off_fa = 0, off_fb = 0, off_cb = 0, off_pa = 0, off_pb = 0,
-         off_zc = 0, off_comp = 0, off_comph = 0, bytes = 0;
+         off_zc = 0, off_comp = 0, off_comph = 0, off_status = 0, bytes = 0;
 };
 
 namespace {
@@ -107,9 +111,11 @@ int32_t validate(const pjzfdtd_problem& p) {
   if (p.out_mode != PJZFDTD_OUT_NONE) {
     if (p.out_step <= 0)
       return fail(PJZFDTD_ERR_INVALID, "output step must be positive");
-    if (p.out_start < 0 || p.out_stop > p.tt)
+    // Steps before 0 are allowed (pjz asks for them when tt is short,
+    // src/pjz/_field.py:216): the field there is the zero initial state.
+    if (p.out_stop > p.tt || p.out_stop <= p.out_start)
       return fail(PJZFDTD_ERR_INVALID,
-                  "output_steps (%d, %d, %d) must lie within [0, tt=%d)",
+                  "output_steps (%d, %d, %d) must end within tt=%d",
                   p.out_start, p.out_stop, p.out_step, p.tt);
   }
   if (p.out_mode == PJZFDTD_OUT_PHASORS || p.out_mode == PJZFDTD_OUT_GRADIENT) {
@@ -129,10 +135,53 @@ int32_t validate(const pjzfdtd_problem& p) {
   return PJZFDTD_OK;
 }
 
-// Resolves the CTA tile: (tile_y + 2) * zz cells, one thread each, at most
-// kMaxThreads threads.
+constexpr size_t kSmemBudget = 220 * 1024;  // of the 227 KB per CTA
+constexpr int kStreamThreads = 512;
+
+// Streamed kernel: zz % 4 == 0, threads = zz * rows-per-pass, and a tile
+// height whose stage ring fits the shared-memory budget.
+int32_t resolve_stream(pjzfdtd_plan* pl) {
+  const int Z = pl->p.zz;
+  const int P = pl->p.pml_lo + pl->p.pml_hi;
+  const int rpt = std::max(1, kStreamThreads / Z);
+  const int S = pl->p.stages > 0 ? pl->p.stages : 4;
+  if (S < 2 || S > 8)
+    return fail(PJZFDTD_ERR_INVALID, "stages must be in [2, 8], got %d", S);
+  int ty = pl->p.tile_y;
+  if (ty == 0) {
+    int best = 0;
+    for (int t = 1; t <= 64; ++t) {
+      if (StreamGeom(t, Z, P).bytes(S) > kSmemBudget) break;
+      // Prefer heights whose H rows split evenly over the row groups.
+      if ((t + 1) % rpt == 0 || t + 1 < rpt || best == 0) best = t;
+    }
+    ty = std::min(best, pl->p.yy);
+  }
+  if (ty <= 0 || StreamGeom(ty, Z, P).bytes(S) > kSmemBudget)
+    return fail(PJZFDTD_ERR_INVALID,
+                "streamed tile (tile_y=%d, zz=%d, stages=%d) exceeds shared "
+                "memory", ty, Z, S);
+  pl->tile_y = ty;
+  pl->stages = S;
+  pl->threads = Z * std::min(rpt, ty + 1);
+  pl->smem = StreamGeom(ty, Z, P).bytes(S);
+  pl->kernel = 2;
+  return PJZFDTD_OK;
+}
+
+// Resolves the CTA tile.  Register-marching kernel: (tile_y + 2) * zz
+// cells, one thread each, at most kMaxThreads threads.
 int32_t resolve_tile(pjzfdtd_plan* pl) {
   const int Z = pl->p.zz;
+  if (pl->p.kernel < 0 || pl->p.kernel > 2)
+    return fail(PJZFDTD_ERR_INVALID, "unknown kernel %d", pl->p.kernel);
+  if (pl->p.kernel == 2 && (Z % 4 != 0 || Z > kStreamThreads))
+    return fail(PJZFDTD_ERR_INVALID,
+                "the streamed kernel needs zz %% 4 == 0 and zz <= %d",
+                kStreamThreads);
+  if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= kStreamThreads))
+    return resolve_stream(pl);
+  pl->kernel = 1;
   int ty = pl->p.tile_y;
   const int max_rows = kMaxThreads / Z;
   if (max_rows < 3)
@@ -146,6 +195,7 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   pl->tile_y = ty;
   pl->threads = ((ty + 2) * Z + 31) / 32 * 32;
   pl->steps_per_pass = 1;
+  pl->smem = 6 * (size_t)(ty + 2) * Z * sizeof(float);
   return PJZFDTD_OK;
 }
 
@@ -172,7 +222,24 @@ void layout(pjzfdtd_plan* pl) {
   if (p.out_mode == PJZFDTD_OUT_GRADIENT) comp = 3 * G;
   pl->off_comp = take(std::max<size_t>(comp, 1) * sizeof(float));
   pl->off_comph = take(std::max<size_t>(p.record_h ? comp : 0, 1) * sizeof(float));
+  pl->off_status = take(sizeof(int));
   pl->bytes = o;
+}
+
+cudaError_t set_stream_smem(size_t bytes) {
+  const int b = (int)bytes;
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecNone>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+    return e;
+  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecSnap>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+    return e;
+  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecProj>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
+    return e;
+  return cudaFuncSetAttribute(yee_stream_kernel<kRecGrad>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, b);
 }
 
 int32_t resolve_seg_x(pjzfdtd_plan* pl) {
@@ -185,9 +252,14 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 1;
-  const size_t smem = 6 * (size_t)(pl->tile_y + 2) * pl->p.zz * sizeof(float);
-  CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-      &per_sm, yee_step_kernel<kRecNone>, pl->threads, smem));
+  if (pl->kernel == 2) {
+    CUDA_TRY(set_stream_smem(pl->smem));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, yee_stream_kernel<kRecNone>, pl->threads, pl->smem));
+  } else {
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, yee_step_kernel<kRecNone>, pl->threads, pl->smem));
+  }
   per_sm = std::max(per_sm, 1);
   const int tiles_y = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
   const int slots = sms * per_sm;
@@ -248,6 +320,11 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   const size_t G = (size_t)p.grad_nx * p.grad_ny * p.grad_nz;
 
   if (n0 == 0) {
+    if (p.out_mode == PJZFDTD_OUT_SNAPSHOTS && p.out_start < 0) {
+      const size_t n = (size_t)pl->ns * 3 * R * sizeof(float);
+      CUDA_TRY(cudaMemsetAsync(b->out, 0, n, st));
+      if (p.record_h) CUDA_TRY(cudaMemsetAsync(b->out_h, 0, n, st));
+    }
     CUDA_TRY(cudaMemcpyAsync(zc, pl->zc.data(), pl->zc.size() * sizeof(float),
                              cudaMemcpyHostToDevice, st));
     if (b->fields)
@@ -324,7 +401,13 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
 
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
-  const size_t smem = 6 * (size_t)(pl->tile_y + 2) * p.zz * sizeof(float);
+  const size_t smem = pl->smem;
+  int* status = at<int>(ws, pl->off_status);
+  if (n0 == 0) CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
+  if (pl->kernel == 2) CUDA_TRY(set_stream_smem(smem));
+  StreamArgs sa;
+  sa.stages = pl->stages;
+  sa.status = status;
   for (int n = n0; n < n1; ++n) {
     const bool even = (n % 2) == 0;
     a.fin = even ? fa : fb;
@@ -343,6 +426,25 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
       } else {
         for (int r = 0; r < p.out_rows; ++r) a.w[r] = pl->weights[(size_t)r * pl->ns + j];
       }
+    }
+    if (pl->kernel == 2) {
+      sa.s = a;
+      switch (rec) {
+        case kRecNone:
+          yee_stream_kernel<kRecNone><<<grid, pl->threads, smem, st>>>(sa);
+          break;
+        case kRecSnap:
+          yee_stream_kernel<kRecSnap><<<grid, pl->threads, smem, st>>>(sa);
+          break;
+        case kRecProj:
+          yee_stream_kernel<kRecProj><<<grid, pl->threads, smem, st>>>(sa);
+          break;
+        default:
+          yee_stream_kernel<kRecGrad><<<grid, pl->threads, smem, st>>>(sa);
+          break;
+      }
+      CUDA_TRY(cudaGetLastError());
+      continue;
     }
     switch (rec) {
       case kRecNone:
@@ -451,12 +553,33 @@ int32_t pjzfdtd_plan_num_samples(const pjzfdtd_plan* plan, int32_t* ns) {
 
 int32_t pjzfdtd_plan_launch_config(const pjzfdtd_plan* plan, int32_t* tile_y,
                                    int32_t* seg_x, int32_t* threads,
-                                   int32_t* steps_per_pass) {
+                                   int32_t* steps_per_pass, int32_t* kernel,
+                                   int32_t* stages) {
   if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
   if (tile_y) *tile_y = plan->tile_y;
   if (seg_x) *seg_x = plan->seg_x > 0 ? plan->seg_x : plan->p.seg_x;
   if (threads) *threads = plan->threads;
   if (steps_per_pass) *steps_per_pass = plan->steps_per_pass;
+  if (kernel) *kernel = plan->kernel;
+  if (stages) *stages = plan->stages;
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_plan_status(pjzfdtd_plan* plan, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
+  if (!workspace || workspace_bytes < plan->bytes)
+    return fail(PJZFDTD_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int* dev = at<int>(workspace, plan->off_status);
+  int host = 0;
+  CUDA_TRY(cudaMemcpyAsync(&host, dev, sizeof(int), cudaMemcpyDeviceToHost, st));
+  CUDA_TRY(cudaStreamSynchronize(st));
+  if (host != 0) {
+    CUDA_TRY(cudaMemsetAsync(dev, 0, sizeof(int), st));
+    return fail(PJZFDTD_ERR_TIMEOUT,
+                "a device-side wait exceeded its limit (status %d)", host);
+  }
   return PJZFDTD_OK;
 }
 

@@ -58,7 +58,8 @@ class Plan:
                out_mode: int = OUT_NONE, weights=None, record_h: bool = False,
                grad_origin: Tuple[int, int, int] = (0, 0, 0),
                grad_shape: Tuple[int, int, int] = (0, 0, 0),
-               tile_y: int = 0, seg_x: int = 0, steps_per_pass: int = 0):
+               tile_y: int = 0, seg_x: int = 0, steps_per_pass: int = 0,
+               kernel: int = 0, stages: int = 0):
     lib = _lib.load()
     p = _lib.Problem()
     p.xx, p.yy, p.zz = (int(v) for v in domain)
@@ -76,6 +77,7 @@ class Plan:
     p.grad_x0, p.grad_y0, p.grad_z0 = (int(v) for v in grad_origin)
     p.grad_nx, p.grad_ny, p.grad_nz = (int(v) for v in grad_shape)
     p.tile_y, p.seg_x, p.steps_per_pass = int(tile_y), int(seg_x), int(steps_per_pass)
+    p.kernel, p.stages = int(kernel), int(stages)
     zz = p.zz
     kap, sig, alp = (_f32_host(a) for a in (pml_kappa, pml_sigma, pml_alpha))
     for name, a in (("pml_kappa", kap), ("pml_sigma", sig), ("pml_alpha", alp)):
@@ -134,11 +136,23 @@ class Plan:
     return None
 
   def launch_config(self):
-    vals = [ctypes.c_int32() for _ in range(4)]
+    vals = [ctypes.c_int32() for _ in range(6)]
     _lib.check(self._lib.pjzfdtd_plan_launch_config(
         self._h, *(ctypes.byref(v) for v in vals)))
-    return dict(zip(("tile_y", "seg_x", "threads", "steps_per_pass"),
-                    (v.value for v in vals)))
+    return dict(zip(("tile_y", "seg_x", "threads", "steps_per_pass", "kernel",
+                     "stages"), (v.value for v in vals)))
+
+  def check_status(self, device=None):
+    """Raises TimeoutError if a bounded device-side wait of the work queued
+    so far gave up (synchronises torch's current stream)."""
+    if self._ws is None:
+      return
+    dev = device or self._ws.device
+    with torch.cuda.device(dev):
+      stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+      _lib.check(self._lib.pjzfdtd_plan_status(
+          self._h, ctypes.c_void_p(self._ws.data_ptr()), self._ws.numel(),
+          stream))
 
   def workspace(self, device) -> torch.Tensor:
     if self._ws is None or self._ws.device != torch.device(device):

@@ -67,8 +67,14 @@ def test_plan_create_host_only(lib):
   X, Y, Z = p.domain
   assert p.workspace_bytes >= (15 * X * Y * Z) * 4
   cfg = p.launch_config()
-  assert cfg["tile_y"] >= 1 and cfg["threads"] % 32 == 0
+  assert cfg["kernel"] == 2 and cfg["stages"] >= 2  # zz % 4 == 0: streamed
+  assert 1 <= cfg["tile_y"] <= Y and cfg["threads"] % Z == 0
+  q = _plan(kernel=1)
+  cfg = q.launch_config()
+  assert cfg["kernel"] == 1 and cfg["threads"] % 32 == 0
   assert (cfg["tile_y"] + 2) * Z <= cfg["threads"]
+  r = _plan(Z=18, region=(16, 14, 14), source_shape=(2, 18, 18))
+  assert r.launch_config()["kernel"] == 1  # zz % 4 != 0 falls back
 
 
 @pytest.mark.parametrize("bad,msg", [
@@ -77,6 +83,7 @@ def test_plan_create_host_only(lib):
     (dict(dt=-1.0), "dt must be positive"),
     (dict(source_origin=(19, 0, 0)), "source box"),
     (dict(output_steps=(30, 60, 5)), "output_steps"),
+    (dict(output_steps=(30, 30, 5)), "output_steps"),
     (dict(output_steps=(30, 50, 0)), "output step"),
     (dict(pml_kappa=np.zeros((16, 2))), "kappa > 0"),
     (dict(pml_sigma=-np.ones((16, 2))), "sigma >= 0"),
@@ -90,8 +97,10 @@ def test_plan_create_rejects(lib, bad, msg):
 
 def test_thick_z_is_unsupported_not_silent(lib):
   with pytest.raises(NotImplementedError, match="thin-z"):
-    _plan(Z=400, region=(16, 14, 300), offset=(2, 2, 2),
-          source_shape=(2, 18, 400))
+    _plan(Z=401, region=(16, 14, 300), offset=(2, 2, 2),
+          source_shape=(2, 18, 401))
+  with pytest.raises(ValueError, match="zz % 4"):
+    _plan(kernel=2, Z=18, region=(16, 14, 14), source_shape=(2, 18, 18))
 
 
 def test_kappa_inf_allowed(lib):
@@ -103,3 +112,9 @@ def test_last_error_is_thread_local_message(lib):
   with pytest.raises(ValueError):
     _plan(dt=0.0)
   assert "dt" in _lib.last_error()
+
+
+def test_negative_output_start_is_allowed(lib):
+  # pjz asks for samples before step 0 when tt < 2 * interval * ww + 1.
+  p = _plan(output_steps=(-12, 50, 9))
+  assert p.num_samples == len(range(-12, 50, 9))

@@ -25,7 +25,7 @@ def dev(a):
 
 
 def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
-            tile_y=0, seg_x=0, fields=None, split=None):
+            tile_y=0, seg_x=0, fields=None, split=None, kernel=0, stages=0):
   p = engine.Plan(domain=case["domain"], offset=case["offset"],
                   region=case["eps"].shape[1:], tt=case["tt"], dt=case["dt"],
                   pml_widths=case["pml_widths"], pml_kappa=case["kappa"],
@@ -35,7 +35,7 @@ def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
                   source_ncols=case["source_profile"].shape[0],
                   output_steps=case["output_steps"], out_mode=out_mode,
                   weights=weights, record_h=record_h, tile_y=tile_y,
-                  seg_x=seg_x)
+                  seg_x=seg_x, kernel=kernel, stages=stages)
   args = dict(epsilon=dev(case["eps"]), absorption_mask=dev(case["mask"]),
               source=dev(case["source_profile"]), waveform=dev(case["waveform"]))
   f = None if fields is None else dev(fields)
@@ -46,62 +46,88 @@ def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
     out, out_h = p.run(**args, fields=f, out=out, out_h=out_h,
                        steps=(split, case["tt"]))
   torch.cuda.synchronize()
+  p.check_status()
   cpu = lambda t: None if t is None else t.cpu().numpy()
   return cpu(out), cpu(out_h), cpu(f)
 
 
+KERNELS = [1, 2]  # register-marching, bulk-copy streamed
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("src", ["x", "y", "z"])
 @pytest.mark.parametrize("Z,pml", [(16, (2, 2)), (24, (3, 5)), (48, (8, 8)),
                                    (64, (8, 8)), (12, (0, 0))])
-def test_snapshots_bit_exact(native, src, Z, pml):
+def test_snapshots_bit_exact(native, src, Z, pml, kernel):
   case = random_problem(hash((src, Z)) % 1000, Z=Z, pml=pml, src=src,
                         src_pos=5 if src == "z" else 7)
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case)
+  got, _, _ = gpu_run(case, kernel=kernel)
   assert np.array_equal(got, want), np.abs(got - want).max()
 
 
-def test_use_z_as_batch_bit_exact(native):
-  case = random_problem(3, Z=20, batch=True, pml=(0, 0))
+def test_odd_z_uses_register_marching_kernel(native):
+  case = random_problem(11, Z=18, pml=(3, 2))
   want = oracle.run(**oracle_kwargs(case))["out"]
   got, _, _ = gpu_run(case)
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("tile_y,seg_x", [(1, 1), (2, 3), (5, 24), (7, 8), (0, 2)])
-def test_launch_geometry_does_not_change_results(native, tile_y, seg_x):
-  case = random_problem(4, X=26, Y=23, Z=16)
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_use_z_as_batch_bit_exact(native, kernel):
+  case = random_problem(3, Z=20, batch=True, pml=(0, 0))
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, tile_y=tile_y, seg_x=seg_x)
+  got, _, _ = gpu_run(case, kernel=kernel)
   assert np.array_equal(got, want)
 
 
-def test_record_h_and_final_state(native):
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("tile_y,seg_x", [(1, 1), (2, 3), (5, 24), (7, 8), (0, 2)])
+def test_launch_geometry_does_not_change_results(native, tile_y, seg_x, kernel):
+  case = random_problem(4, X=26, Y=23, Z=16)
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, tile_y=tile_y, seg_x=seg_x, kernel=kernel)
+  assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("stages", [2, 3, 5, 8])
+def test_stream_ring_depth_does_not_change_results(native, stages):
+  case = random_problem(12, X=30, Y=21, Z=32, pml=(4, 4))
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, kernel=2, stages=stages, tile_y=6, seg_x=7)
+  assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_record_h_and_final_state(native, kernel):
   case = random_problem(5, Z=24, pml=(4, 4))
   f0 = np.random.default_rng(9).normal(size=(6,) + case["domain"]).astype(np.float32)
   want = oracle.run(**oracle_kwargs(case), record_h=True, fields=f0.copy())
-  got, got_h, got_f = gpu_run(case, record_h=True, fields=f0.copy())
+  got, got_h, got_f = gpu_run(case, record_h=True, fields=f0.copy(),
+                              kernel=kernel)
   assert np.array_equal(got, want["out"])
   assert np.array_equal(got_h, want["out_h"])
   assert np.array_equal(got_f, want["fields"])
 
 
-def test_run_steps_chaining_matches_single_run(native):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_run_steps_chaining_matches_single_run(native, kernel):
   case = random_problem(6, tt=60, steps=(20, 60, 7))
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, split=33)
+  got, _, _ = gpu_run(case, split=33, kernel=kernel)
   assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("rows", [2, 10, 32])
-def test_phasor_projection_bit_exact(native, rows):
+def test_phasor_projection_bit_exact(native, rows, kernel):
   case = random_problem(7, Z=32, pml=(4, 4), steps=(10, 48, 3))
   ns = len(range(*case["output_steps"]))
   w = np.random.default_rng(rows).normal(size=(rows, ns)).astype(np.float32)
   want = oracle.run(**oracle_kwargs(case), mode="project", weights=w,
                     record_h=True)
   got, got_h, _ = gpu_run(case, out_mode=engine.OUT_PHASORS, weights=w,
-                          record_h=True)
+                          record_h=True, kernel=kernel)
   assert np.array_equal(got, want["out"])
   assert np.array_equal(got_h, want["out_h"])
 
@@ -162,7 +188,8 @@ def test_field_c0_full_vs_fp32_and_fp64_oracle(native):
   assert err < 1e-5
 
 
-def test_c1_size_short_run_bit_exact(native):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_c1_size_short_run_bit_exact(native, kernel):
   """Full 512x512x64 domain for 24 steps against the FP32 oracle."""
   wl = workloads.design_c1(tt=24, ww=5)
   sp = wl.sim_params
@@ -178,7 +205,7 @@ def test_c1_size_short_run_bit_exact(native):
               source_profile=prof, waveform=kw["source_waveform"],
               output_steps=steps, domain=domain)
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case)
+  got, _, _ = gpu_run(case, kernel=kernel)
   assert np.array_equal(got, want)
 
 
