@@ -59,7 +59,10 @@ struct pjzfdtd_plan {
   size_t smem = 0;  // dynamic shared memory per CTA
   // Workspace layout (byte offsets).
   size_t off_fa = 0, off_fb = 0, off_cb = 0, off_pa = 0, off_pb = 0,
-         off_zc = 0, off_comp = 0, off_comph = 0, off_status = 0, bytes = 0;
+         off_zc = 0, off_comp = 0, off_comph = 0, off_status = 0, off_mask = 0,
+         bytes = 0;
+  int Pp = 0;  // PML state row stride (P rounded up to 4)
+  int Yp = 0;  // padded y length of the streamed kernel's absorber copy
 };
 
 namespace {
@@ -138,12 +141,13 @@ int32_t validate(const pjzfdtd_problem& p) {
 constexpr size_t kSmemBudget = 220 * 1024;  // of the 227 KB per CTA
 constexpr int kStreamThreads = 512;
 
-// Streamed kernel: zz % 4 == 0, threads = zz * rows-per-pass, and a tile
-// height whose stage ring fits the shared-memory budget.
+// Streamed kernel: zz % 4 == 0, one compute thread per z-pair of a row,
+// compute threads = (zz / 2) * rows-per-pass rounded up to whole warps, one
+// extra producer warp, and a tile height whose ring fits shared memory.
 int32_t resolve_stream(pjzfdtd_plan* pl) {
   const int Z = pl->p.zz;
   const int P = pl->p.pml_lo + pl->p.pml_hi;
-  const int rpt = std::max(1, kStreamThreads / Z);
+  const int rpt = std::max(1, (kStreamThreads - 32) / (Z / 2));
   const int S = pl->p.stages > 0 ? pl->p.stages : 4;
   if (S < 2 || S > 8)
     return fail(PJZFDTD_ERR_INVALID, "stages must be in [2, 8], got %d", S);
@@ -163,7 +167,8 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
                 "memory", ty, Z, S);
   pl->tile_y = ty;
   pl->stages = S;
-  pl->threads = Z * std::min(rpt, ty + 1);
+  const int ncomp = ((Z / 2) * std::min(rpt, ty + 1) + 31) / 32 * 32;
+  pl->threads = ncomp + 32;
   pl->smem = StreamGeom(ty, Z, P).bytes(S);
   pl->kernel = 2;
   return PJZFDTD_OK;
@@ -175,11 +180,11 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   const int Z = pl->p.zz;
   if (pl->p.kernel < 0 || pl->p.kernel > 2)
     return fail(PJZFDTD_ERR_INVALID, "unknown kernel %d", pl->p.kernel);
-  if (pl->p.kernel == 2 && (Z % 4 != 0 || Z > kStreamThreads))
+  const int zmax = 2 * (kStreamThreads - 32);
+  if (pl->p.kernel == 2 && (Z % 4 != 0 || Z > zmax))
     return fail(PJZFDTD_ERR_INVALID,
-                "the streamed kernel needs zz %% 4 == 0 and zz <= %d",
-                kStreamThreads);
-  if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= kStreamThreads))
+                "the streamed kernel needs zz %% 4 == 0 and zz <= %d", zmax);
+  if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax))
     return resolve_stream(pl);
   pl->kernel = 1;
   int ty = pl->p.tile_y;
@@ -202,7 +207,9 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
 void layout(pjzfdtd_plan* pl) {
   const pjzfdtd_problem& p = pl->p;
   const size_t N = (size_t)pl->N;
-  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->P, 1);
+  pl->Pp = round4(pl->P);
+  pl->Yp = round4(p.yy);
+  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
   const size_t R = (size_t)p.rx * p.ry * p.rz;
   const size_t G = (size_t)p.grad_nx * p.grad_ny * p.grad_nz;
   size_t o = 0;
@@ -223,6 +230,7 @@ void layout(pjzfdtd_plan* pl) {
   pl->off_comp = take(std::max<size_t>(comp, 1) * sizeof(float));
   pl->off_comph = take(std::max<size_t>(p.record_h ? comp : 0, 1) * sizeof(float));
   pl->off_status = take(sizeof(int));
+  pl->off_mask = take((pl->kernel == 2 ? (size_t)p.xx * 3 * pl->Yp : 1) * sizeof(float));
   pl->bytes = o;
 }
 
@@ -307,7 +315,7 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   if (rc) return rc;
   const pjzfdtd_problem& p = pl->p;
   const long long N = pl->N;
-  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->P, 1);
+  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
   float* fa = at<float>(ws, pl->off_fa);
   float* fb = at<float>(ws, pl->off_fb);
   float* cb = at<float>(ws, pl->off_cb);
@@ -354,6 +362,13 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
         b->epsilon, b->absorption_mask, cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
         p.rx, p.ry, p.rz, p.dt);
     CUDA_TRY(cudaGetLastError());
+    if (pl->kernel == 2) {
+      const long long nm = (long long)p.xx * 3 * pl->Yp;
+      pad_mask_kernel<<<(int)std::min<long long>((nm + 255) / 256, 1 << 16), 256, 0,
+                        st>>>(b->absorption_mask, at<float>(ws, pl->off_mask),
+                              p.xx, p.yy, pl->Yp);
+      CUDA_TRY(cudaGetLastError());
+    }
   }
 
   StepArgs a;
@@ -361,7 +376,8 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   a.X = p.xx;
   a.Y = p.yy;
   a.Z = p.zz;
-  a.P = std::max(pl->P, 1);
+  a.P = pl->P;
+  a.Pst = std::max(pl->Pp, 1);
   a.plo = p.pml_lo;
   a.phi = p.pml_hi;
   a.N = N;
@@ -408,6 +424,8 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   StreamArgs sa;
   sa.stages = pl->stages;
   sa.status = status;
+  sa.Yp = pl->Yp;
+  sa.mask_ws = at<float>(ws, pl->off_mask);
   for (int n = n0; n < n1; ++n) {
     const bool even = (n % 2) == 0;
     a.fin = even ? fa : fb;

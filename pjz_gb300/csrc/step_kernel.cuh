@@ -34,6 +34,7 @@ enum RecordMode { kRecNone = 0, kRecSnap = 1, kRecProj = 2, kRecGrad = 3 };
 
 struct StepArgs {
   int X, Y, Z, P, plo, phi;
+  int Pst;  // row stride of the PML state arrays (P rounded up to 4)
   long long N;  // X * Y * Z
   float dt;
   int tile_y, seg_x;
@@ -42,7 +43,7 @@ struct StepArgs {
   const float* __restrict__ cb;    // [3][N]   dt / (eps + sigma dt / 2)
   const float* __restrict__ mask;  // [3][X][Y] absorber conductivity
   const float* __restrict__ zc;    // [6][Z]   ik_e, b_e, c_e, ik_h, b_h, c_h
-  const float* __restrict__ psi_in;  // [4][X][Y][P] hx, hy, ex, ey
+  const float* __restrict__ psi_in;  // [4][X][Y][Pst] hx, hy, ex, ey
   float* __restrict__ psi_out;
   // Source box: J_c = sum_k src[k][c][box] * wave[k].
   int sx0, sy0, sz0, snx, sny, snz, snc;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(kMaxThreads)
   const long long colz = (long long)y * Z + z;
   const int pz = !act ? -1
                       : (z < a.plo ? z : (z >= Z - a.phi ? z - (Z - a.phi) + a.plo : -1));
-  const long long PXY = (long long)X * Y * a.P;
+  const long long PXY = (long long)X * Y * a.Pst;
 
   float ike = 0.f, be = 0.f, ce = 0.f, ikh = 0.f, bh = 0.f, ch = 0.f;
   if (act) {
@@ -163,7 +164,7 @@ __global__ void __launch_bounds__(kMaxThreads)
       const float dEy_x = fsub(e1y, e0y), dEx_y = fsub(ex_y1, e0x);
       float zEy, zEx;
       if (pz >= 0) {
-        const long long pi = ((long long)x * Y + y) * a.P + pz;
+        const long long pi = ((long long)x * Y + y) * a.Pst + pz;
         const float na = ffma(ch, dEy_z, fmul(bh, a.psi_in[pi]));
         const float nb = ffma(ch, dEx_z, fmul(bh, a.psi_in[PXY + pi]));
         if (write) {
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(kMaxThreads)
       const float dHy_x = fsub(hy, hyp), dHx_y = fsub(hx, hx_ym);
       float zHy, zHx;
       if (pz >= 0) {
-        const long long pi = ((long long)x * Y + y) * a.P + pz;
+        const long long pi = ((long long)x * Y + y) * a.Pst + pz;
         const float na = ffma(ce, dHy_z, fmul(be, a.psi_in[2 * PXY + pi]));
         const float nb = ffma(ce, dHx_z, fmul(be, a.psi_in[3 * PXY + pi]));
         a.psi_out[2 * PXY + pi] = na;

@@ -1,24 +1,34 @@
 // Streamed Yee step kernel for sm_103a: the same single-step update as
-// yee_step_kernel, with every x-plane tile staged into shared memory by the
-// bulk-copy engine (cp.async.bulk + mbarrier) several planes ahead.
+// yee_step_kernel, with every x-plane tile moved by the bulk-copy engine.
 //
 // A CTA owns `tile_y` rows of y (all of z) and marches through `seg_x`
-// x-planes.  For plane x the tile needs E rows -1..TY, H rows -1..TY-1 and
-// the E coefficient rows 0..TY-1; in the [c][x][y][z] layout each of those
-// is one contiguous span per component, so a stage is filled by nine bulk
-// copies issued by one thread and tracked by one mbarrier (transaction
-// bytes).  The per-column absorber conductivity and the z-PML state rows go
-// through cp.async (4-byte, any alignment) in the same stage.  A ring of
-// `stages` slots keeps stages-1 planes in flight while the CTA computes one,
-// so DRAM latency is off the critical path.  H computed for plane x stays in
-// shared memory (double-buffered) as the x-1 neighbour of the next plane.
+// x-planes.  For plane x the tile needs E rows -1..TY, H rows -1..TY-1, the
+// E coefficient rows 0..TY-1, the absorber row and the z-PML state rows; in
+// the workspace layouts ([c][x][y][z] fields, [x][c][Yp] absorber,
+// [c][x][y][Pp] PML state, Yp and Pp padded to multiples of 4) each piece is
+// one contiguous 16-byte aligned span, so one thread fills a ring slot with
+// bulk copies (cp.async.bulk, completion on the slot's mbarrier) `stages`-1
+// planes ahead.  Results go the same way: new H stays in shared memory (it
+// is also the x-1 neighbour of the next plane), new E and PML state are
+// written to shared staging buffers, and one thread bulk-stores them.  No
+// compute thread issues a global load or store on the main path.
 //
-// Requires zz % 4 == 0 (16-byte aligned spans); the host falls back to
-// yee_step_kernel otherwise.  Arithmetic is the same explicit RN sequence,
-// so results are bit-identical to the CPU oracle.
+// Each thread updates a pair of adjacent z cells with 64-bit shared-memory
+// accesses; for zz = 64 a warp covers one full z column of one y row.
+//
+// Requires zz % 4 == 0; the host falls back to yee_step_kernel otherwise.
+// Arithmetic is the same explicit RN sequence as the CPU oracle, so results
+// are bit-identical to it.
+//
+// The last warp of the CTA is a producer that issues every bulk copy and
+// store; the other warps only compute, synchronised with the producer by
+// mbarriers and among themselves by a named barrier, so the serial issue of
+// copies never sits between two compute phases.
 //
 // Every wait is bounded: an mbarrier wait that exceeds kWaitCycles sets the
-// status word and the whole CTA leaves at the next barrier.
+// status word and the abort flag, the compute warps leave together at their
+// next named barrier, and the producer drains the copies it issued (again
+// with bounded waits) before the CTA exits.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,7 +44,9 @@ constexpr int kStatusTimeout = 4;
 struct StreamArgs {
   StepArgs s;
   int stages;
-  int* status;  // device status word (0 = ok)
+  int Yp;                                 // padded y length of mask_ws rows
+  const float* __restrict__ mask_ws;      // [X][3][Yp]
+  int* status;                            // device status word (0 = ok)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -89,43 +101,92 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src,
       : "memory");
 }
 
-__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)),
-               "l"(src)
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src,
+                                         uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(
+                   dst),
+               "r"(smem_u32(src)), "r"(bytes)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
 }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
 }
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__host__ __device__ inline int round4(int v) { return (v + 3) & ~3; }
 
 // Shared-memory geometry of one CTA (floats unless noted).
 struct StreamGeom {
-  int TY, Z, P, RE, RH;
-  int e_off, h_off, c_off, m_off, p_off, stage;  // within a stage
+  int TY, Z, P, Pp, RE, RH, MT;
+  int e_off, h_off, c_off, m_off, p_off, stage;  // within a ring slot
   __host__ __device__ StreamGeom(int ty, int z, int p) {
     TY = ty;
     Z = z;
     P = p;
+    Pp = round4(p);
     RE = ty + 2;
     RH = ty + 1;
+    MT = round4(ty) + 8;  // 4-aligned window around rows y0..y0+TY-1
     e_off = 0;
     h_off = e_off + 3 * RE * z;
     c_off = h_off + 3 * RH * z;
     m_off = c_off + 3 * ty * z;
-    p_off = m_off + ((3 * ty + 3) & ~3);
-    stage = p_off + ((4 * RH * p + 3) & ~3);
+    p_off = m_off + 3 * MT;
+    stage = p_off + 4 * RH * Pp;
   }
+  // CTA buffers after the ring: new H [2][3][RH*Z], new E [2][3][TY*Z],
+  // new PML state [2][4][TY*Pp].
   __host__ __device__ size_t hn_floats() const { return 2 * 3 * (size_t)RH * Z; }
+  __host__ __device__ size_t en_floats() const { return 2 * 3 * (size_t)TY * Z; }
+  __host__ __device__ size_t pn_floats() const { return 2 * 4 * (size_t)TY * Pp; }
   __host__ __device__ size_t bytes(int stages) const {
-    return ((size_t)stages * stage + hn_floats()) * sizeof(float) +
-           (size_t)stages * sizeof(uint64_t) + 16;
+    return ((size_t)stages * stage + hn_floats() + en_floats() + pn_floats()) *
+               sizeof(float) +
+           (size_t)(2 * stages + 2) * sizeof(uint64_t) + 16;
   }
 };
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// Bounded wait that also gives up when another thread of the CTA already
+// did (`*abort` set); returns false in either case.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity,
+                                                   int* status,
+                                                   volatile int* abort) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const long long t0 = clock64();
+  for (;;) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (*abort) return false;
+    if (clock64() - t0 > kWaitCycles) {
+      atomicExch(status, kStatusTimeout);
+      *abort = 1;
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void compute_sync(int nthreads) {
+  asm volatile("bar.sync 1, %0;" ::"r"(nthreads) : "memory");
+}
+
+// Warp-specialised CTA: the last warp is the producer (bulk loads into the
+// ring, bulk stores of results), all other warps compute.  Barriers:
+//   full[s]  -- ring slot s holds its plane (producer expect_tx + copies);
+//   done[s]  -- every compute warp finished the plane in slot s, whose
+//               results sit in output buffer b = (x - x0) & 1 (count = warps);
+//   free[b]  -- the producer's bulk stores finished reading buffer b.
 template <int REC>
 __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) float sm[];
@@ -133,16 +194,23 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   const int X = a.X, Y = a.Y, Z = a.Z, TY = a.tile_y;
   const int S = sa.stages;
   const StreamGeom g(TY, Z, a.plo + a.phi);
-  const int P = g.P;
-  float* hn = sm + (size_t)S * g.stage;  // [2][3][RH*Z]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(hn + g.hn_floats());
+  const int Pp = g.Pp;
+  float* hn = sm + (size_t)S * g.stage;   // [2][3][RH*Z]
+  float* en = hn + g.hn_floats();         // [2][3][TY*Z]
+  float* pn = en + g.en_floats();         // [2][4][TY*Pp]
+  uint64_t* full = reinterpret_cast<uint64_t*>(pn + g.pn_floats());
+  uint64_t* done = full + S;
+  uint64_t* freeb = done + S;
   __shared__ int abort_flag;
 
   const int tid = threadIdx.x;
-  const int nt = blockDim.x;
-  const int z = tid % Z;
-  const int rt = tid / Z;
-  const int rpt = nt / Z;
+  const int ncomp = blockDim.x - 32;      // compute threads (multiple of 32)
+  const int nwarps = ncomp >> 5;
+  const bool producer = tid >= ncomp;
+  const int Zh = Z >> 1;
+  const int rpt = ncomp / Zh;             // rows per pass
+  const int z0 = 2 * (tid % Zh);
+  const int rt = tid / Zh;                // >= rpt: idle compute thread
   const int y0 = blockIdx.x * TY;
   const int xs = blockIdx.y * a.seg_x;
   const int xe = min(X, xs + a.seg_x);
@@ -150,262 +218,361 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   const int xlast = min(xe, X - 1);  // last plane whose E is read
   const long long N = a.N;
   const long long YZ = (long long)Y * Z;
-  const long long PXY = (long long)X * Y * max(P, 1);
-  // Valid y rows of the E halo tile [y0-1, y0+TY] and the H tile
-  // [y0-1, y0+TY-1] and the coefficient rows [y0, y0+TY-1].
+  const long long PXY = (long long)X * Y * Pp;
   const int ey_lo = max(y0 - 1, 0), ey_hi = min(y0 + TY + 1, Y);
   const int hy_hi = min(y0 + TY, Y);
-  const int cy_hi = min(y0 + TY, Y);
+  const int nrows = hy_hi - y0;           // owned rows inside the domain
+  const int erow0 = ey_lo - (y0 - 1);     // tile row of the first valid row
+  const int ma = y0 & ~3;                 // absorber window start
+  const int mb = min(round4(y0 + TY), sa.Yp);
+  const int moff = y0 - ma;
+  const int RHZ = g.RH * Z, REZ = g.RE * Z;
 
   if (tid == 0) {
     abort_flag = 0;
-    for (int s = 0; s < S; ++s) mbar_init(&bars[s], 1);
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&done[s], nwarps);
+    }
+    mbar_init(&freeb[0], 1);
+    mbar_init(&freeb[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // Zero every slot and both H buffers once: rows outside the domain are
-  // never overwritten and read as the zero boundary.
-  for (size_t i = tid; i < (size_t)S * g.stage + g.hn_floats(); i += nt) sm[i] = 0.f;
+  // Rows outside the domain are never written and read as the zero boundary.
+  for (size_t i = tid; i < (size_t)S * g.stage + g.hn_floats() + g.en_floats() +
+                               g.pn_floats();
+       i += blockDim.x)
+    sm[i] = 0.f;
+  fence_async_smem();
   __syncthreads();
 
-  const int pz = z < a.plo ? z : (z >= Z - a.phi ? z - (Z - a.phi) + a.plo : -1);
-  const float ike = a.zc[z], be = a.zc[Z + z], ce = a.zc[2 * Z + z];
-  const float ikh = a.zc[3 * Z + z], bh = a.zc[4 * Z + z], ch = a.zc[5 * Z + z];
-  const float mdt = -a.dt;
-
-  // Issues the copies of plane xp into slot `slot` (E only when !full).
-  auto fill = [&](int xp, int slot, bool full) {
-    float* st = sm + (size_t)slot * g.stage;
-    if (tid == 0) {
+  if (producer) {
+    if ((tid & 31) != 0) return;
+    // ---------------- producer (one lane) ----------------
+    auto fill = [&](int xp, int slot, bool fullp) {
+      float* st = sm + (size_t)slot * g.stage;
       const uint32_t eb = (uint32_t)((ey_hi - ey_lo) * Z * 4);
       const uint32_t hb = (uint32_t)((hy_hi - ey_lo) * Z * 4);
-      const uint32_t cbb = (uint32_t)((cy_hi - y0) * Z * 4);
-      uint32_t total = 3 * eb + (full ? 3 * (hb + cbb) : 0);
-      mbar_expect_tx(&bars[slot], total);
+      const uint32_t cbb = (uint32_t)(nrows * Z * 4);
+      const uint32_t mbb = (uint32_t)((mb - ma) * 4);
+      const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
+      const uint32_t total =
+          3 * eb + (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
+      mbar_expect_tx(&full[slot], total);
       const long long base = (long long)xp * YZ;
-      const int erow0 = ey_lo - (y0 - 1);
       for (int c = 0; c < 3; ++c)
-        bulk_g2s(st + g.e_off + c * g.RE * Z + erow0 * Z,
-                 a.fin + c * N + base + (long long)ey_lo * Z, eb, &bars[slot]);
-      if (full) {
+        bulk_g2s(st + g.e_off + c * REZ + erow0 * Z,
+                 a.fin + c * N + base + (long long)ey_lo * Z, eb, &full[slot]);
+      if (!fullp) return;
+      for (int c = 0; c < 3; ++c) {
+        bulk_g2s(st + g.h_off + c * RHZ + erow0 * Z,
+                 a.fin + (3 + c) * N + base + (long long)ey_lo * Z, hb, &full[slot]);
+        bulk_g2s(st + g.c_off + c * TY * Z, a.cb + c * N + base + (long long)y0 * Z,
+                 cbb, &full[slot]);
+        bulk_g2s(st + g.m_off + c * g.MT,
+                 sa.mask_ws + ((long long)xp * 3 + c) * sa.Yp + ma, mbb, &full[slot]);
+      }
+      if (Pp > 0)
+        for (int c = 0; c < 4; ++c)
+          bulk_g2s(st + g.p_off + c * g.RH * Pp + erow0 * Pp,
+                   a.psi_in + c * PXY + ((long long)xp * Y + ey_lo) * Pp, pb,
+                   &full[slot]);
+    };
+    int nfill = 0;  // planes issued so far (x0 + nfill is the next one)
+    while (nfill < S && x0 + nfill <= xlast) {
+      fill(x0 + nfill, nfill, x0 + nfill < xe);
+      ++nfill;
+    }
+    bool ok = true;
+    for (int x = x0; x < xe && ok; ++x) {
+      const int k = x - x0;
+      const int slot = k % S;
+      const uint32_t round = (uint32_t)(k / S);
+      const int b = k & 1;
+      ok = mbar_wait_or_abort(&done[slot], round & 1, sa.status, &abort_flag);
+      if (!ok) break;
+      if (x >= xs) {
+        float* hcur = hn + (size_t)b * 3 * RHZ;
+        float* ecur = en + (size_t)b * 3 * TY * Z;
+        float* pcur = pn + (size_t)b * 4 * TY * Pp;
+        const long long base = (long long)x * YZ + (long long)y0 * Z;
+        const uint32_t fb = (uint32_t)(nrows * Z * 4);
         for (int c = 0; c < 3; ++c) {
-          bulk_g2s(st + g.h_off + c * g.RH * Z + erow0 * Z,
-                   a.fin + (3 + c) * N + base + (long long)ey_lo * Z, hb,
-                   &bars[slot]);
-          bulk_g2s(st + g.c_off + c * TY * Z,
-                   a.cb + c * N + base + (long long)y0 * Z, cbb, &bars[slot]);
+          bulk_s2g(a.fout + (3 + c) * N + base, hcur + c * RHZ + Z, fb);
+          bulk_s2g(a.fout + c * N + base, ecur + c * TY * Z, fb);
         }
-      }
-    }
-    if (full) {
-      // Absorber conductivity of rows y0..y0+TY-1 and z-PML state of rows
-      // y0-1..y0+TY-1 for plane xp.
-      const long long XY = (long long)X * Y;
-      for (int i = tid; i < 3 * TY; i += nt) {
-        const int c = i / TY, r = i - c * TY;
-        if (y0 + r < Y)
-          cp_async4(st + g.m_off + i, a.mask + c * XY + (long long)xp * Y + y0 + r);
-      }
-      if (P > 0) {
-        const int n = 4 * g.RH * P;
-        for (int i = tid; i < n; i += nt) {
-          const int c = i / (g.RH * P);
-          const int rem = i - c * g.RH * P;
-          const int r = rem / P, q = rem - r * P;
-          const int y = y0 - 1 + r;
-          if (y >= 0 && y < Y)
-            cp_async4(st + g.p_off + i,
-                      a.psi_in + c * PXY + ((long long)xp * Y + y) * P + q);
+        if (Pp > 0) {
+          const uint32_t pb = (uint32_t)(nrows * Pp * 4);
+          const long long pbase = ((long long)x * Y + y0) * Pp;
+          for (int c = 0; c < 4; ++c)
+            bulk_s2g(a.psi_out + c * PXY + pbase, pcur + c * TY * Pp, pb);
         }
+        bulk_commit();
       }
+      // Slot of plane x is free: refill it with the next plane.
+      if (x0 + nfill <= xlast) {
+        fill(x0 + nfill, slot, x0 + nfill < xe);
+        ++nfill;
+      }
+      bulk_wait_read_all();
+      mbar_arrive(&freeb[b]);
     }
-    cp_async_commit();
-  };
-
-  // Prologue: planes x0 .. x0+S-1 (those that exist).
-  for (int k = 0; k < S; ++k) {
-    const int xp = x0 + k;
-    if (xp <= xlast) fill(xp, k, xp < xe);
-    else cp_async_commit();
+    // Drain: every issued fill must land before shared memory is released.
+    for (int j = max(0, nfill - S); j < nfill; ++j)
+      mbar_wait_or_abort(&full[j % S], (uint32_t)(j / S) & 1, sa.status,
+                         &abort_flag);
+    bulk_wait_all();
+    return;
   }
 
-  int slot = 0;  // slot of plane x
-  uint32_t round = 0;  // fill round of plane x's slot
-  bool waited_first = false;
+  // ---------------- compute warps ----------------
+  int pz[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int z = z0 + k;
+    pz[k] = z < a.plo ? z : (z >= Z - a.phi ? z - (Z - a.phi) + a.plo : -1);
+  }
+  float ike[2], be[2], ce[2], ikh[2], bh[2], ch[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int z = z0 + k;
+    ike[k] = a.zc[z];
+    be[k] = a.zc[Z + z];
+    ce[k] = a.zc[2 * Z + z];
+    ikh[k] = a.zc[3 * Z + z];
+    bh[k] = a.zc[4 * Z + z];
+    ch[k] = a.zc[5 * Z + z];
+  }
+  const bool zpml = pz[0] >= 0 || pz[1] >= 0;
+  const float mdt = -a.dt;
+  const bool active = rt < rpt;
+
   for (int x = x0; x < xe; ++x) {
-    const int slot1 = (slot + 1 == S) ? 0 : slot + 1;
-    const uint32_t round1 = (slot + 1 == S) ? round + 1 : round;
+    const int k = x - x0;
+    const int slot = k % S;
+    const int slot1 = (k + 1) % S;
+    const uint32_t round = (uint32_t)(k / S);
+    const uint32_t round1 = (uint32_t)((k + 1) / S);
+    const int b = k & 1;
     const bool has_x1 = x + 1 < X;
     bool ok = true;
-    if (!waited_first) {
-      ok = mbar_wait(&bars[slot], round & 1, sa.status);
-      waited_first = true;
-    }
-    if (ok && has_x1) ok = mbar_wait(&bars[slot1], round1 & 1, sa.status);
-    if (!ok) abort_flag = 1;
+    if (k == 0) ok = mbar_wait_or_abort(&full[slot], round & 1, sa.status, &abort_flag);
+    if (ok && has_x1)
+      ok = mbar_wait_or_abort(&full[slot1], round1 & 1, sa.status, &abort_flag);
+    if (ok && k >= 2)
+      ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
+                              &abort_flag);
 
     const float* st = sm + (size_t)slot * g.stage;
-    const float* st1 = sm + (size_t)slot1 * g.stage;
     const float* Es = st + g.e_off;
-    const float* E1 = st1 + g.e_off;
+    const float* E1 = sm + (size_t)slot1 * g.stage + g.e_off;
     const float* Hs = st + g.h_off;
     const float* Cs = st + g.c_off;
-    const float* Ms = st + g.m_off;
+    const float* Ms = st + g.m_off + moff;
     const float* Ps = st + g.p_off;
-    float* hcur = hn + (size_t)(x & 1) * 3 * g.RH * Z;
-    const float* hprev = hn + (size_t)((x + 1) & 1) * 3 * g.RH * Z;
+    float* hcur = hn + (size_t)b * 3 * RHZ;
+    const float* hprev = hn + (size_t)(b ^ 1) * 3 * RHZ;
+    float* ecur = en + (size_t)b * 3 * TY * Z;
+    float* pcur = pn + (size_t)b * 4 * TY * Pp;
     const bool wr = x >= xs;
 
-    // H^{n+1/2}(x) for rows -1..TY-1.
-    if (ok) {
+    // H^{n+1/2}(x) for tile rows 0..TY (y = y0-1 .. y0+TY-1).
+    if (ok && active) {
       for (int r = rt; r < g.RH; r += rpt) {
         const int y = y0 - 1 + r;
         if (y < 0 || y >= Y) continue;
-        const int ie = r * Z + z;
-        const float e0x = Es[ie], e0y = Es[g.RE * Z + ie], e0z = Es[2 * g.RE * Z + ie];
-        const float ex_y1 = Es[ie + Z], ez_y1 = Es[2 * g.RE * Z + ie + Z];
-        const float ex_z1 = (z + 1 < Z) ? Es[ie + 1] : 0.f;
-        const float ey_z1 = (z + 1 < Z) ? Es[g.RE * Z + ie + 1] : 0.f;
-        const float e1y = has_x1 ? E1[g.RE * Z + ie] : 0.f;
-        const float e1z = has_x1 ? E1[2 * g.RE * Z + ie] : 0.f;
-        const float dEz_y = fsub(ez_y1, e0z), dEy_z = fsub(ey_z1, e0y);
-        const float dEx_z = fsub(ex_z1, e0x), dEz_x = fsub(e1z, e0z);
-        const float dEy_x = fsub(e1y, e0y), dEx_y = fsub(ex_y1, e0x);
-        float zEy, zEx;
-        if (pz >= 0) {
-          const float na = ffma(ch, dEy_z, fmul(bh, Ps[r * P + pz]));
-          const float nb = ffma(ch, dEx_z, fmul(bh, Ps[g.RH * P + r * P + pz]));
-          if (wr && r > 0) {
-            const long long pi = ((long long)x * Y + y) * P + pz;
-            a.psi_out[pi] = na;
-            a.psi_out[PXY + pi] = nb;
+        const int ie = r * Z + z0;
+        const float2 ex = *reinterpret_cast<const float2*>(Es + ie);
+        const float2 ey = *reinterpret_cast<const float2*>(Es + REZ + ie);
+        const float2 ez = *reinterpret_cast<const float2*>(Es + 2 * REZ + ie);
+        const float2 ex_y1 = *reinterpret_cast<const float2*>(Es + ie + Z);
+        const float2 ez_y1 = *reinterpret_cast<const float2*>(Es + 2 * REZ + ie + Z);
+        const bool zin = z0 + 2 < Z;
+        const float ex_z2 = zin ? Es[ie + 2] : 0.f;
+        const float ey_z2 = zin ? Es[REZ + ie + 2] : 0.f;
+        float2 e1y = make_float2(0.f, 0.f), e1z = make_float2(0.f, 0.f);
+        if (has_x1) {
+          e1y = *reinterpret_cast<const float2*>(E1 + REZ + ie);
+          e1z = *reinterpret_cast<const float2*>(E1 + 2 * REZ + ie);
+        }
+        const float2 hox = *reinterpret_cast<const float2*>(Hs + ie);
+        const float2 hoy = *reinterpret_cast<const float2*>(Hs + RHZ + ie);
+        const float2 hoz = *reinterpret_cast<const float2*>(Hs + 2 * RHZ + ie);
+        const float exs[2] = {ex.x, ex.y}, eys[2] = {ey.x, ey.y}, ezs[2] = {ez.x, ez.y};
+        const float exy1[2] = {ex_y1.x, ex_y1.y}, ezy1[2] = {ez_y1.x, ez_y1.y};
+        const float exz1[2] = {ex.y, ex_z2}, eyz1[2] = {ey.y, ey_z2};
+        const float e1ys[2] = {e1y.x, e1y.y}, e1zs[2] = {e1z.x, e1z.y};
+        const float hos[3][2] = {{hox.x, hox.y}, {hoy.x, hoy.y}, {hoz.x, hoz.y}};
+        float hnew[3][2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float dEz_y = fsub(ezy1[q], ezs[q]), dEy_z = fsub(eyz1[q], eys[q]);
+          const float dEx_z = fsub(exz1[q], exs[q]), dEz_x = fsub(e1zs[q], ezs[q]);
+          const float dEy_x = fsub(e1ys[q], eys[q]), dEx_y = fsub(exy1[q], exs[q]);
+          float zEy, zEx;
+          if (zpml && pz[q] >= 0) {
+            const int pi = r * Pp + pz[q];
+            const float na = ffma(ch[q], dEy_z, fmul(bh[q], Ps[pi]));
+            const float nb = ffma(ch[q], dEx_z, fmul(bh[q], Ps[g.RH * Pp + pi]));
+            if (r > 0) {
+              pcur[(r - 1) * Pp + pz[q]] = na;
+              pcur[TY * Pp + (r - 1) * Pp + pz[q]] = nb;
+            }
+            zEy = ffma(dEy_z, ikh[q], na);
+            zEx = ffma(dEx_z, ikh[q], nb);
+          } else {
+            zEy = fmul(dEy_z, ikh[q]);
+            zEx = fmul(dEx_z, ikh[q]);
           }
-          zEy = ffma(dEy_z, ikh, na);
-          zEx = ffma(dEx_z, ikh, nb);
-        } else {
-          zEy = fmul(dEy_z, ikh);
-          zEx = fmul(dEx_z, ikh);
+          hnew[0][q] = ffma(mdt, fsub(dEz_y, zEy), hos[0][q]);
+          hnew[1][q] = ffma(mdt, fsub(zEx, dEz_x), hos[1][q]);
+          hnew[2][q] = ffma(mdt, fsub(dEy_x, dEx_y), hos[2][q]);
         }
-        const int ih = r * Z + z;
-        const float hx = ffma(mdt, fsub(dEz_y, zEy), Hs[ih]);
-        const float hy = ffma(mdt, fsub(zEx, dEz_x), Hs[g.RH * Z + ih]);
-        const float hz = ffma(mdt, fsub(dEy_x, dEx_y), Hs[2 * g.RH * Z + ih]);
-        hcur[ih] = hx;
-        hcur[g.RH * Z + ih] = hy;
-        hcur[2 * g.RH * Z + ih] = hz;
-        if (wr && r > 0) {
-          const long long i = x * YZ + (long long)y * Z + z;
-          a.fout[3 * N + i] = hx;
-          a.fout[4 * N + i] = hy;
-          a.fout[5 * N + i] = hz;
-        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          *reinterpret_cast<float2*>(hcur + c * RHZ + ie) =
+              make_float2(hnew[c][0], hnew[c][1]);
       }
     }
-    __syncthreads();
+    compute_sync(ncomp);
     if (abort_flag) break;
 
-    // E^{n+1}(x) for rows 0..TY-1.
-    if (wr) {
+    // E^{n+1}(x) for rows 0..TY-1 (y = y0 .. y0+TY-1).
+    const bool src_plane = x >= a.sx0 && x < a.sx0 + a.snx;
+    if (wr && active) {
       for (int r = rt; r < TY; r += rpt) {
         const int y = y0 + r;
         if (y >= Y) continue;
-        const int ih = (r + 1) * Z + z;  // H tile index of this row
-        const float hx = hcur[ih], hy = hcur[g.RH * Z + ih], hz = hcur[2 * g.RH * Z + ih];
-        const float hx_ym = hcur[ih - Z], hz_ym = hcur[2 * g.RH * Z + ih - Z];
-        const float hx_zm = z > 0 ? hcur[ih - 1] : 0.f;
-        const float hy_zm = z > 0 ? hcur[g.RH * Z + ih - 1] : 0.f;
-        const float hyp = hprev[g.RH * Z + ih], hzp = hprev[2 * g.RH * Z + ih];
-        const float dHz_y = fsub(hz, hz_ym), dHy_z = fsub(hy, hy_zm);
-        const float dHx_z = fsub(hx, hx_zm), dHz_x = fsub(hz, hzp);
-        const float dHy_x = fsub(hy, hyp), dHx_y = fsub(hx, hx_ym);
-        const long long i = x * YZ + (long long)y * Z + z;
-        float zHy, zHx;
-        if (pz >= 0) {
-          const int pr = (r + 1) * P + pz;
-          const float na = ffma(ce, dHy_z, fmul(be, Ps[2 * g.RH * P + pr]));
-          const float nb = ffma(ce, dHx_z, fmul(be, Ps[3 * g.RH * P + pr]));
-          const long long pi = ((long long)x * Y + y) * P + pz;
-          a.psi_out[2 * PXY + pi] = na;
-          a.psi_out[3 * PXY + pi] = nb;
-          zHy = ffma(dHy_z, ike, na);
-          zHx = ffma(dHx_z, ike, nb);
-        } else {
-          zHy = fmul(dHy_z, ike);
-          zHx = fmul(dHx_z, ike);
-        }
-        float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
-        if (x >= a.sx0 && x < a.sx0 + a.snx && y >= a.sy0 && y < a.sy0 + a.sny &&
-            z >= a.sz0 && z < a.sz0 + a.snz) {
-          const long long sb = (long long)a.snx * a.sny * a.snz;
-          const long long si =
-              ((long long)(x - a.sx0) * a.sny + (y - a.sy0)) * a.snz + (z - a.sz0);
+        const int ih = (r + 1) * Z + z0;
+        const float2 hx = *reinterpret_cast<const float2*>(hcur + ih);
+        const float2 hy = *reinterpret_cast<const float2*>(hcur + RHZ + ih);
+        const float2 hz = *reinterpret_cast<const float2*>(hcur + 2 * RHZ + ih);
+        const float2 hx_ym = *reinterpret_cast<const float2*>(hcur + ih - Z);
+        const float2 hz_ym = *reinterpret_cast<const float2*>(hcur + 2 * RHZ + ih - Z);
+        const bool zin = z0 > 0;
+        const float hx_zm = zin ? hcur[ih - 1] : 0.f;
+        const float hy_zm = zin ? hcur[RHZ + ih - 1] : 0.f;
+        const float2 hyp = *reinterpret_cast<const float2*>(hprev + RHZ + ih);
+        const float2 hzp = *reinterpret_cast<const float2*>(hprev + 2 * RHZ + ih);
+        const float2 eox = *reinterpret_cast<const float2*>(Es + ih);
+        const float2 eoy = *reinterpret_cast<const float2*>(Es + REZ + ih);
+        const float2 eoz = *reinterpret_cast<const float2*>(Es + 2 * REZ + ih);
+        const int ic = r * Z + z0;
+        const float2 cbx = *reinterpret_cast<const float2*>(Cs + ic);
+        const float2 cby = *reinterpret_cast<const float2*>(Cs + TY * Z + ic);
+        const float2 cbz = *reinterpret_cast<const float2*>(Cs + 2 * TY * Z + ic);
+        const float sig[3] = {Ms[r], Ms[g.MT + r], Ms[2 * g.MT + r]};
+        const float hxs[2] = {hx.x, hx.y}, hys[2] = {hy.x, hy.y}, hzs[2] = {hz.x, hz.y};
+        const float hxym[2] = {hx_ym.x, hx_ym.y}, hzym[2] = {hz_ym.x, hz_ym.y};
+        const float hxzm[2] = {hx_zm, hx.x}, hyzm[2] = {hy_zm, hy.x};
+        const float hyps[2] = {hyp.x, hyp.y}, hzps[2] = {hzp.x, hzp.y};
+        const float eo[3][2] = {{eox.x, eox.y}, {eoy.x, eoy.y}, {eoz.x, eoz.y}};
+        const float cbs[3][2] = {{cbx.x, cbx.y}, {cby.x, cby.y}, {cbz.x, cbz.y}};
+        float enew[3][2];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float j = 0.f;
-            for (int k = 0; k < a.snc; ++k)
-              j = ffma(a.src[((long long)k * 3 + c) * sb + si], a.wave[k], j);
-            cur[c] = fsub(cur[c], j);
+        for (int q = 0; q < 2; ++q) {
+          const int z = z0 + q;
+          const float dHz_y = fsub(hzs[q], hzym[q]), dHy_z = fsub(hys[q], hyzm[q]);
+          const float dHx_z = fsub(hxs[q], hxzm[q]), dHz_x = fsub(hzs[q], hzps[q]);
+          const float dHy_x = fsub(hys[q], hyps[q]), dHx_y = fsub(hxs[q], hxym[q]);
+          float zHy, zHx;
+          if (zpml && pz[q] >= 0) {
+            const int pi = (r + 1) * Pp + pz[q];
+            const float na = ffma(ce[q], dHy_z, fmul(be[q], Ps[2 * g.RH * Pp + pi]));
+            const float nb = ffma(ce[q], dHx_z, fmul(be[q], Ps[3 * g.RH * Pp + pi]));
+            pcur[2 * TY * Pp + r * Pp + pz[q]] = na;
+            pcur[3 * TY * Pp + r * Pp + pz[q]] = nb;
+            zHy = ffma(dHy_z, ike[q], na);
+            zHx = ffma(dHx_z, ike[q], nb);
+          } else {
+            zHy = fmul(dHy_z, ike[q]);
+            zHx = fmul(dHx_z, ike[q]);
           }
-        }
-        const int ie = (r + 1) * Z + z;
-        const int ic = r * Z + z;
-        float e_new[3];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float eo = Es[c * g.RE * Z + ie];
-          const float rr = ffma(-Ms[c * TY + r], eo, cur[c]);
-          e_new[c] = ffma(Cs[c * TY * Z + ic], rr, eo);
-          a.fout[c * N + i] = e_new[c];
-        }
-        if (REC == kRecSnap || REC == kRecProj) {
-          const int qx = x - a.ox, qy = y - a.oy, qz = z - a.oz;
-          if (qx >= 0 && qx < a.rx && qy >= 0 && qy < a.ry && qz >= 0 && qz < a.rz) {
-            const long long R = (long long)a.rx * a.ry * a.rz;
-            const long long ri = ((long long)qx * a.ry + qy) * a.rz + qz;
-            const float hnew[3] = {hx, hy, hz};
+          float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
+          if (src_plane && y >= a.sy0 && y < a.sy0 + a.sny && z >= a.sz0 &&
+              z < a.sz0 + a.snz) {
+            const long long sb = (long long)a.snx * a.sny * a.snz;
+            const long long si =
+                ((long long)(x - a.sx0) * a.sny + (y - a.sy0)) * a.snz + (z - a.sz0);
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-              if (REC == kRecSnap) {
-                a.out[c * R + ri] = e_new[c];
-                if (a.record_h) a.out_h[c * R + ri] = hnew[c];
-              } else {
-                for (int rr = 0; rr < a.rows; ++rr) {
-                  const long long ai = ((long long)rr * 3 + c) * R + ri;
-                  kahan(&a.out[ai], &a.comp[ai], a.w[rr], e_new[c]);
-                  if (a.record_h) kahan(&a.out_h[ai], &a.comp_h[ai], a.w[rr], hnew[c]);
+              float j = 0.f;
+              for (int w = 0; w < a.snc; ++w)
+                j = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], j);
+              cur[c] = fsub(cur[c], j);
+            }
+          }
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float rr = ffma(-sig[c], eo[c][q], cur[c]);
+            enew[c][q] = ffma(cbs[c][q], rr, eo[c][q]);
+          }
+          if (REC == kRecSnap || REC == kRecProj) {
+            const int qx = x - a.ox, qy = y - a.oy, qz = z - a.oz;
+            if (qx >= 0 && qx < a.rx && qy >= 0 && qy < a.ry && qz >= 0 && qz < a.rz) {
+              const long long R = (long long)a.rx * a.ry * a.rz;
+              const long long ri = ((long long)qx * a.ry + qy) * a.rz + qz;
+              const float hs3[3] = {hxs[q], hys[q], hzs[q]};
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                if (REC == kRecSnap) {
+                  a.out[c * R + ri] = enew[c][q];
+                  if (a.record_h) a.out_h[c * R + ri] = hs3[c];
+                } else {
+                  for (int w = 0; w < a.rows; ++w) {
+                    const long long ai = ((long long)w * 3 + c) * R + ri;
+                    kahan(&a.out[ai], &a.comp[ai], a.w[w], enew[c][q]);
+                    if (a.record_h) kahan(&a.out_h[ai], &a.comp_h[ai], a.w[w], hs3[c]);
+                  }
                 }
               }
             }
           }
-        }
-        if (REC == kRecGrad) {
-          const int gx = x - a.gx0, gy = y - a.gy0, gz = z - a.gz0;
-          if (gx >= 0 && gx < a.gnx && gy >= 0 && gy < a.gny && gz >= 0 && gz < a.gnz) {
-            const long long G = (long long)a.gnx * a.gny * a.gnz;
-            const long long gi = ((long long)gx * a.gny + gy) * a.gnz + gz;
+          if (REC == kRecGrad) {
+            const int gx = x - a.gx0, gy = y - a.gy0, gz = z - a.gz0;
+            if (gx >= 0 && gx < a.gnx && gy >= 0 && gy < a.gny && gz >= 0 && gz < a.gnz) {
+              const long long G = (long long)a.gnx * a.gny * a.gnz;
+              const long long gi = ((long long)gx * a.gny + gy) * a.gnz + gz;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              float coef = 0.f;
-              for (int rr = 0; rr < a.rows; ++rr)
-                coef = ffma(a.w[rr], a.q[((long long)rr * 3 + c) * G + gi], coef);
-              kahan(&a.out[c * G + gi], &a.comp[c * G + gi], coef, e_new[c]);
+              for (int c = 0; c < 3; ++c) {
+                float coef = 0.f;
+                for (int w = 0; w < a.rows; ++w)
+                  coef = ffma(a.w[w], a.q[((long long)w * 3 + c) * G + gi], coef);
+                kahan(&a.out[c * G + gi], &a.comp[c * G + gi], coef, enew[c][q]);
+              }
             }
           }
         }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          *reinterpret_cast<float2*>(ecur + c * TY * Z + ic) =
+              make_float2(enew[c][0], enew[c][1]);
       }
     }
-    // Plane x+1's cp.async pieces must land before anyone reads them.
-    cp_async_wait<0>();
-    __syncthreads();
-    // Slot of plane x is free: refill it with plane x+S.
-    const int xn = x + S;
-    if (xn <= xlast) {
-      if (tid == 0) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      fill(xn, slot, xn < xe);
-    }
-    slot = slot1;
-    round = round1;
+    // Publish this plane's results to the producer (bulk stores read them
+    // through the async proxy) and release its ring slot.
+    fence_async_smem();
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&done[slot]);
+    // H(x-1) (hprev) is rewritten by the next plane's H phase.
+    compute_sync(ncomp);
   }
-  cp_async_wait<0>();
+}
+
+// Absorber conductivity re-laid out as [x][c][Yp] (Yp % 4 == 0, zero tail)
+// so each (x, c) row of a tile is one aligned span.
+__global__ void pad_mask_kernel(const float* __restrict__ mask,
+                                float* __restrict__ mask_ws, int X, int Y,
+                                int Yp) {
+  const long long n = (long long)X * 3 * Yp;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(t % Yp);
+    const long long xc = t / Yp;
+    const int c = (int)(xc % 3);
+    const int x = (int)(xc / 3);
+    mask_ws[t] = y < Y ? mask[((long long)c * X + x) * Y + y] : 0.f;
+  }
 }
 
 }  // namespace pjzfdtd

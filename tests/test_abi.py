@@ -68,7 +68,7 @@ def test_plan_create_host_only(lib):
   assert p.workspace_bytes >= (15 * X * Y * Z) * 4
   cfg = p.launch_config()
   assert cfg["kernel"] == 2 and cfg["stages"] >= 2  # zz % 4 == 0: streamed
-  assert 1 <= cfg["tile_y"] <= Y and cfg["threads"] % Z == 0
+  assert 1 <= cfg["tile_y"] <= Y and cfg["threads"] % 32 == 0
   q = _plan(kernel=1)
   cfg = q.launch_config()
   assert cfg["kernel"] == 1 and cfg["threads"] % 32 == 0
