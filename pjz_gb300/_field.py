@@ -16,7 +16,7 @@ from typing import Any, NamedTuple, Tuple
 import numpy as np
 import torch
 
-from . import engine
+from . import _adjoint, engine
 from ._fdtdz import LaunchParams, cached_plan, launch_knobs, _key_array
 
 
@@ -261,6 +261,81 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
   return plan, prof
 
 
+def _launch_dict(launch_params):
+  k = launch_knobs(launch_params)
+  return dict(tile_y=k.tile_y, seg_x=k.seg_x, steps_per_pass=k.steps_per_pass,
+              kernel=k.kernel, stages=k.stages)
+
+
+class _FieldFn(torch.autograd.Function):
+  """``field`` with a fused adjoint backward (no time history).
+
+  Forward runs over the whole domain with epsilon edge-extended (what the
+  engine does outside the region anyway) so that the backward sees every
+  cell an epsilon voxel feeds; backward runs one adjoint solve, adds the
+  source-plane term of pjz's source division by epsilon, and folds the
+  domain gradient back onto the region.
+  """
+
+  @staticmethod
+  def forward(ctx, epsilon, source, omega, source_pos, sim_params):
+    kw, om = _setup(epsilon, source, omega, source_pos, sim_params)
+    mask = kw["absorption_mask"]
+    domain = (int(mask.shape[1]), int(mask.shape[2]), int(kw["pml_kappa"].shape[0]))
+    offset = kw["offset"]
+    region = tuple(int(v) for v in epsilon.shape[1:])
+    eps_dom = _adjoint.extend_epsilon(epsilon.detach(), domain, offset)
+    kw_dom = dict(kw, epsilon=eps_dom, offset=(0, 0, 0))
+    plan, prof = phasor_plan(kw_dom, om)
+    out, _ = plan.run(epsilon=eps_dom, absorption_mask=mask, source=prof,
+                      waveform=kw["source_waveform"])
+    ww = om.shape[0]
+    F = torch.complex(out[:ww], out[ww:])
+    ctx.save_for_backward(F, eps_dom)
+    ctx.kw = kw
+    ctx.omega = om
+    ctx.prof = prof
+    ctx.domain, ctx.region, ctx.offset = domain, region, offset
+    ctx.sim_params = sim_params
+    sl = tuple(slice(o, o + s) for o, s in zip(offset, region))
+    return F[(slice(None), slice(None)) + sl].contiguous()
+
+  @staticmethod
+  def backward(ctx, g_region):
+    F, eps_dom = ctx.saved_tensors
+    kw, om, sp = ctx.kw, ctx.omega, ctx.sim_params
+    dt = float(kw["dt"])
+    X, Y, Z = ctx.domain
+    ww = om.shape[0]
+    g = torch.zeros((ww, 3, X, Y, Z), dtype=torch.complex64, device=F.device)
+    sl = tuple(slice(o, o + s) for o, s in zip(ctx.offset, ctx.region))
+    g[(slice(None), slice(None)) + sl] = g_region.to(torch.complex64)
+    weights = projection_weights(om, kw["output_steps"], dt)
+    # pjz divides the source by epsilon at the source plane (_field.py:219).
+    origin, shape, prof = engine.plane_source_box(
+        kw["source_field"], kw["source_position"], ctx.domain)
+    wph = _adjoint.waveform_phasors(kw["source_waveform"].cpu().numpy(),
+                                    kw["output_steps"], om, dt, weights)
+    wt = _adjoint.discrete_omega(om, dt)
+    coef = torch.as_tensor(1j * wt * np.exp(-1.5j * om * dt), dtype=torch.complex64,
+                           device=F.device)
+    wphs = torch.as_tensor(wph, dtype=torch.complex64, device=F.device)
+    bsl = tuple(slice(o, o + s) for o, s in zip(origin, shape))
+    jh = torch.einsum("kcxyz,kw->wcxyz", prof.to(torch.complex64), wphs)
+    src_term = torch.zeros_like(g)
+    src_term[(slice(None), slice(None)) + bsl] = (
+        coef[:, None, None, None, None] * jh / eps_dom[(slice(None),) + bsl])
+    grad = _adjoint.run_adjoint(
+        g=g, F=F, omega=om, dt=dt, tt=int(sp.tt), ramp_width=sp.source_ramp,
+        ramp_delay=sp.source_delay, weights=weights,
+        output_steps=kw["output_steps"], epsilon_domain=eps_dom,
+        absorption_mask=kw["absorption_mask"], pml_widths=kw["pml_widths"],
+        pml_kappa=kw["pml_kappa"], pml_sigma=kw["pml_sigma"],
+        pml_alpha=kw["pml_alpha"], src_term=src_term,
+        launch=_launch_dict(kw["launch_params"]))
+    return _adjoint.fold_to_region(grad, ctx.region, ctx.offset), None, None, None, None
+
+
 def field(
     epsilon,
     source,
@@ -279,11 +354,14 @@ def field(
 
   Returns:
     ``(ww, 3, xx, yy, zz)`` complex64 fields at ``omega`` on epsilon's device.
+    Differentiable w.r.t. ``epsilon`` (one fused adjoint solve per backward).
   """
   dev = (epsilon.device if isinstance(epsilon, torch.Tensor) and epsilon.is_cuda
          else torch.device("cuda"))
   epsilon = _to_device(epsilon, dev).to(torch.float32)
   source = _to_device(source, dev)
+  if torch.is_grad_enabled() and epsilon.requires_grad:
+    return _FieldFn.apply(epsilon, source, omega, source_pos, sim_params)
   kw, omega = _setup(epsilon, source, omega, source_pos, sim_params)
   plan, prof = phasor_plan(kw, omega)
   out, _ = plan.run(epsilon=epsilon, absorption_mask=kw["absorption_mask"],

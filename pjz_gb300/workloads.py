@@ -143,3 +143,29 @@ def design_c1(tt: int = 10000, domain=(512, 512, 64), absorber: int = 16,
   return Workload(f"c1 design {X}x{Y}x{Z}", eps.astype(np.float32), src, omega,
                   20 - absorber, sp, tuple(domain),
                   ((x0, y0, z0), (dx, dy, dz)))
+
+
+def port_profile(wl: Workload, sigma: float = 7.5) -> np.ndarray:
+  """Gaussian port (sigma 7.5 cells = 300 nm) centred on the waveguide,
+  ``(yy, zz)`` over the epsilon region's transverse plane."""
+  _, _, yy, zz = wl.epsilon.shape
+  return _gaussian_sheet(yy, zz, yy / 2, zz / 2, sigma).astype(np.float32)
+
+
+def output_plane(wl: Workload) -> int:
+  """x index (epsilon region frame) of the output monitor plane."""
+  return wl.epsilon.shape[1] - 20
+
+
+def overlap_objective(fields, wl: Workload, port=None, dtype=None):
+  """c2 objective: ``sum_w |sum_{y,z} port * E_y(x_out)|^2`` of ``field``'s
+  output ``(ww, 3, xx, yy, zz)`` (torch complex); ``dtype`` (e.g.
+  complex128) sets the precision of the reduction."""
+  import torch
+  p = port if port is not None else torch.as_tensor(
+      port_profile(wl), device=fields.device)
+  e = fields[:, 1, output_plane(wl)]
+  if dtype is not None:
+    e, p = e.to(dtype), p.to(dtype)
+  ov = (e * p).sum(dim=(-2, -1))
+  return (ov.abs() ** 2).sum()

@@ -1,0 +1,142 @@
+"""GPU adjoint: ``field``'s autograd backward (one fused adjoint solve)
+against central finite differences.
+
+* small cases: the whole gradient against the same adjoint restated in FP64
+  on the CPU oracle, and FD of the FP64 oracle forward (exact arithmetic)
+  at interior, region-boundary (edge-extended) and source-plane voxels;
+* c2: the 512x512x64 c1 geometry, objective sum_w |port . E_y(x_out)|^2,
+  16 seeded design voxels, FD (delta-eps 1e-3) of the GPU FP32 forward.
+Tolerance: 1e-3 relative (vector norm over the checked voxels).
+"""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from oracle import adjoint as oradj
+from oracle import pjz_ref
+import pjz_gb300
+from pjz_gb300 import workloads
+from pjz_gb300._fdtdz import LaunchParams
+
+pytestmark = pytest.mark.gpu
+DEV = torch.device("cuda:0")
+
+
+def _small(isolated=True, tt=4000):
+  """Small pjz problem: a scatterer (isolated, or a waveguide running into
+  the absorber), an x-normal source at an odd position (bumped, flipped
+  columns) and a monitor cotangent on a plane."""
+  rng = np.random.default_rng(3)
+  xx, yy, zz = 22, 18, 8
+  eps = np.full((3, xx, yy, zz), 2.1, np.float32)
+  if isolated:
+    eps[:, 8:14, 6:12, 2:6] = 9.0
+  else:
+    eps[:, :, 6:12, 2:6] = 9.0
+  eps[:, 9:13, 7:11, 2:6] += rng.uniform(-1, 1, (3, 4, 4, 4)).astype(np.float32)
+  src = np.zeros((2, 1, yy, zz), np.float32)
+  src[0, 0, 6:12, 2:6] = 1.0
+  omega = np.array([2 * np.pi / 20, 2 * np.pi / 18])
+  sp = pjz_gb300.SimParams(omega_range=(omega.min(), omega.max()), tt=tt,
+                           source_ramp=float(omega.mean() * 0.5 * 150),
+                           source_delay=3.0, absorption_padding=10,
+                           absorption_coeff=3e-3, pml_widths=(3, 3),
+                           use_reduced_precision=False,
+                           launch_params=LaunchParams(zz=16))
+  c = np.zeros((2, 3, xx, yy, zz), complex)
+  c[:, 1, 18, 5:13, 1:7] = rng.normal(size=(2, 8, 6)) + 1j * rng.normal(size=(2, 8, 6))
+  return eps, src, omega, 3, sp, c
+
+
+# interior, source plane (x = 3), region edges (edge-extended into the
+# absorber and the z-PML).
+POINTS = [(1, 11, 9, 4), (0, 10, 8, 3), (2, 12, 10, 4), (1, 3, 8, 3),
+          (1, 3, 10, 4), (1, 0, 9, 3), (1, 21, 9, 4), (0, 11, 0, 3),
+          (2, 11, 9, 7)]
+
+
+def _gpu_grad(eps, src, omega, pos, sp, c):
+  e = torch.tensor(eps, device=DEV, requires_grad=True)
+  F = pjz_gb300.field(e, torch.as_tensor(src, device=DEV), omega, pos, sp)
+  ct = torch.as_tensor(c, dtype=torch.complex64, device=DEV)
+  torch.real(torch.sum(torch.conj(ct) * F)).backward()
+  return F.detach().cpu().numpy(), e.grad.cpu().numpy()
+
+
+def _oracle_sp(sp):
+  return pjz_ref.SimParams(*sp[:-1])
+
+
+@pytest.mark.parametrize("isolated", [True, False])
+def test_field_backward_matches_fp64_oracle_adjoint(native, isolated):
+  """Same adjoint method in FP64 on the CPU oracle: the whole gradient."""
+  eps, src, omega, pos, sp, c = _small(isolated, tt=2500)
+  _, got = _gpu_grad(eps, src, omega, pos, sp, c)
+  _, want = oradj.field_and_gradient(eps, src, omega, pos, _oracle_sp(sp), c, zz=16)
+  err = np.linalg.norm(got - want) / np.linalg.norm(want)
+  print("GPU FP32 adjoint vs FP64 oracle adjoint: rel-L2", err)
+  assert err < 1e-4
+
+
+def test_field_backward_vs_fp64_finite_differences(native):
+  """Converging geometry: adjoint vs central differences of the FP64
+  oracle forward (delta-eps 1e-3), 1e-3 relative."""
+  eps, src, omega, pos, sp, c = _small(True)
+  _, grad = _gpu_grad(eps, src, omega, pos, sp, c)
+  loss = lambda e: np.real(np.sum(np.conj(c) * oradj.field_and_gradient(
+      e, src, omega, pos, _oracle_sp(sp), c, zz=16, with_gradient=False)[0]))
+  fd = []
+  for p in POINTS:
+    d = 1e-3
+    ep, em = eps.copy(), eps.copy()
+    ep[p] += d
+    em[p] -= d
+    fd.append((loss(ep) - loss(em)) / (2 * d))
+  fd = np.array(fd)
+  ad = np.array([grad[p] for p in POINTS])
+  err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
+  print("small adjoint vs FP64 FD:", err, fd, ad)
+  assert err < 1e-3
+
+
+def test_c2_gradient_vs_fd_16_voxels(native):
+  """c2: c1 geometry, sum_w |overlap|^2 objective, 16 seeded design voxels."""
+  wl = workloads.design_c1()
+  eps = torch.tensor(wl.epsilon, device=DEV, requires_grad=True)
+  src = torch.as_tensor(wl.source, device=DEV)
+  port = torch.as_tensor(workloads.port_profile(wl), device=DEV)
+  F = pjz_gb300.field(eps, src, wl.omega, wl.source_pos, wl.sim_params)
+  L = workloads.overlap_objective(F, wl, port)
+  L.backward()
+  grad = eps.grad
+  (bx, by, bz), (nx, ny, nz) = wl.design_box
+  rng = np.random.default_rng(1)
+  pts = [(int(rng.integers(3)), bx + int(rng.integers(nx)),
+          by + int(rng.integers(ny)), bz + int(rng.integers(nz)))
+         for _ in range(16)]
+  fd, ad = [], []
+  with torch.no_grad():
+    base = wl.epsilon
+    for p in pts:
+      d = 1e-3
+      ep, em = base.copy(), base.copy()
+      ep[p] += d
+      em[p] -= d
+      lp = workloads.overlap_objective(
+          pjz_gb300.field(torch.as_tensor(ep, device=DEV), src, wl.omega,
+                          wl.source_pos, wl.sim_params), wl, port,
+          dtype=torch.complex128)
+      lm = workloads.overlap_objective(
+          pjz_gb300.field(torch.as_tensor(em, device=DEV), src, wl.omega,
+                          wl.source_pos, wl.sim_params), wl, port,
+          dtype=torch.complex128)
+      fd.append((lp - lm).item() / (2 * d))
+      ad.append(grad[p].item())
+  fd, ad = np.array(fd), np.array(ad)
+  err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
+  print("c2 adjoint vs FD (16 voxels): rel", err)
+  print("fd", fd)
+  print("adj", ad)
+  assert err < 1e-3
