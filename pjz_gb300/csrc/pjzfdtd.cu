@@ -17,6 +17,7 @@
 #include "../../include/pjzfdtd.h"
 #include "step_kernel.cuh"
 #include "stream_kernel.cuh"
+#include "record_kernel.cuh"
 
 using namespace pjzfdtd;
 
@@ -235,19 +236,9 @@ void layout(pjzfdtd_plan* pl) {
 }
 
 cudaError_t set_stream_smem(size_t bytes) {
-  const int b = (int)bytes;
-  cudaError_t e;
-  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecNone>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
-    return e;
-  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecSnap>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
-    return e;
-  if ((e = cudaFuncSetAttribute(yee_stream_kernel<kRecProj>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize, b)))
-    return e;
-  return cudaFuncSetAttribute(yee_stream_kernel<kRecGrad>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+  return cudaFuncSetAttribute(yee_stream_kernel,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)bytes);
 }
 
 int32_t resolve_seg_x(pjzfdtd_plan* pl) {
@@ -263,10 +254,10 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   if (pl->kernel == 2) {
     CUDA_TRY(set_stream_smem(pl->smem));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, yee_stream_kernel<kRecNone>, pl->threads, pl->smem));
+        &per_sm, yee_stream_kernel, pl->threads, pl->smem));
   } else {
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, yee_step_kernel<kRecNone>, pl->threads, pl->smem));
+        &per_sm, yee_step_kernel, pl->threads, pl->smem));
   }
   per_sm = std::max(per_sm, 1);
   const int tiles_y = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
@@ -395,25 +386,6 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   a.snz = p.src_ncols > 0 ? p.src_nz : 0;
   a.snc = p.src_ncols;
   a.src = b->source;
-  a.record_h = p.record_h;
-  a.ox = p.ox;
-  a.oy = p.oy;
-  a.oz = p.oz;
-  a.rx = p.rx;
-  a.ry = p.ry;
-  a.rz = p.rz;
-  a.out = b->out;
-  a.out_h = b->out_h;
-  a.comp = comp;
-  a.comp_h = comph;
-  a.rows = p.out_rows;
-  a.gx0 = p.grad_x0;
-  a.gy0 = p.grad_y0;
-  a.gz0 = p.grad_z0;
-  a.gnx = p.grad_nx;
-  a.gny = p.grad_ny;
-  a.gnz = p.grad_nz;
-  a.q = b->q;
 
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
@@ -421,6 +393,26 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   int* status = at<int>(ws, pl->off_status);
   if (n0 == 0) CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
   if (pl->kernel == 2) CUDA_TRY(set_stream_smem(smem));
+  RecordArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  ra.N = N;
+  ra.X = p.xx;
+  ra.Y = p.yy;
+  ra.Z = p.zz;
+  if (p.out_mode == PJZFDTD_OUT_GRADIENT) {
+    ra.bx0 = p.grad_x0; ra.by0 = p.grad_y0; ra.bz0 = p.grad_z0;
+    ra.bnx = p.grad_nx; ra.bny = p.grad_ny; ra.bnz = p.grad_nz;
+  } else {
+    ra.bx0 = p.ox; ra.by0 = p.oy; ra.bz0 = p.oz;
+    ra.bnx = p.rx; ra.bny = p.ry; ra.bnz = p.rz;
+  }
+  ra.record_h = p.record_h;
+  ra.out = b->out;
+  ra.out_h = b->out_h;
+  ra.comp = comp;
+  ra.comp_h = comph;
+  ra.rows = p.out_rows;
+  ra.q = b->q;
   StreamArgs sa;
   sa.stages = pl->stages;
   sa.status = status;
@@ -433,52 +425,39 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
     a.psi_in = even ? pa : pb;
     a.psi_out = even ? pb : pa;
     a.wave = p.src_ncols > 0 ? b->waveform + (size_t)n * p.src_ncols : nullptr;
-    int rec = kRecNone;
+    if (pl->kernel == 2) {
+      sa.s = a;
+      yee_stream_kernel<<<grid, pl->threads, smem, st>>>(sa);
+    } else {
+      yee_step_kernel<<<grid, pl->threads, smem, st>>>(a);
+    }
+    CUDA_TRY(cudaGetLastError());
     if (p.out_mode != PJZFDTD_OUT_NONE && n >= p.out_start && n < p.out_stop &&
         (n - p.out_start) % p.out_step == 0) {
       const int j = (n - p.out_start) / p.out_step;
-      rec = p.out_mode;
-      if (rec == kRecSnap) {
-        a.out = b->out + (size_t)j * 3 * R;
-        a.out_h = p.record_h ? b->out_h + (size_t)j * 3 * R : nullptr;
+      ra.f = a.fout;
+      if (p.out_mode == PJZFDTD_OUT_SNAPSHOTS) {
+        ra.out = b->out + (size_t)j * 3 * R;
+        ra.out_h = p.record_h ? b->out_h + (size_t)j * 3 * R : nullptr;
       } else {
-        for (int r = 0; r < p.out_rows; ++r) a.w[r] = pl->weights[(size_t)r * pl->ns + j];
+        for (int r = 0; r < p.out_rows; ++r)
+          ra.w[r] = pl->weights[(size_t)r * pl->ns + j];
       }
-    }
-    if (pl->kernel == 2) {
-      sa.s = a;
-      switch (rec) {
-        case kRecNone:
-          yee_stream_kernel<kRecNone><<<grid, pl->threads, smem, st>>>(sa);
+      const long long nb = (long long)ra.bnx * ra.bny * ra.bnz;
+      const int rblocks = (int)std::min<long long>((nb + 255) / 256, 1 << 20);
+      switch (p.out_mode) {
+        case PJZFDTD_OUT_SNAPSHOTS:
+          record_kernel<kRecSnap><<<rblocks, 256, 0, st>>>(ra);
           break;
-        case kRecSnap:
-          yee_stream_kernel<kRecSnap><<<grid, pl->threads, smem, st>>>(sa);
-          break;
-        case kRecProj:
-          yee_stream_kernel<kRecProj><<<grid, pl->threads, smem, st>>>(sa);
+        case PJZFDTD_OUT_PHASORS:
+          record_kernel<kRecProj><<<rblocks, 256, 0, st>>>(ra);
           break;
         default:
-          yee_stream_kernel<kRecGrad><<<grid, pl->threads, smem, st>>>(sa);
+          record_kernel<kRecGrad><<<rblocks, 256, 0, st>>>(ra);
           break;
       }
       CUDA_TRY(cudaGetLastError());
-      continue;
     }
-    switch (rec) {
-      case kRecNone:
-        yee_step_kernel<kRecNone><<<grid, pl->threads, smem, st>>>(a);
-        break;
-      case kRecSnap:
-        yee_step_kernel<kRecSnap><<<grid, pl->threads, smem, st>>>(a);
-        break;
-      case kRecProj:
-        yee_step_kernel<kRecProj><<<grid, pl->threads, smem, st>>>(a);
-        break;
-      default:
-        yee_step_kernel<kRecGrad><<<grid, pl->threads, smem, st>>>(a);
-        break;
-    }
-    CUDA_TRY(cudaGetLastError());
   }
   if (n1 == p.tt && b->fields) {
     float* fin = (p.tt % 2 == 0) ? fa : fb;

@@ -49,17 +49,6 @@ struct StepArgs {
   int sx0, sy0, sz0, snx, sny, snz, snc;
   const float* __restrict__ src;
   const float* __restrict__ wave;  // row of the waveform for this step
-  // Recording (this step is sample `sample` when record != kRecNone).
-  int record_h;
-  int ox, oy, oz, rx, ry, rz;
-  float* __restrict__ out;
-  float* __restrict__ out_h;
-  float* __restrict__ comp;
-  float* __restrict__ comp_h;
-  int rows;
-  int gx0, gy0, gz0, gnx, gny, gnz;
-  const float* __restrict__ q;
-  float w[kMaxRows];
 };
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
@@ -78,7 +67,6 @@ __device__ __forceinline__ void kahan(float* s, float* c, float w, float e) {
   *s = t;
 }
 
-template <int REC>
 __global__ void __launch_bounds__(kMaxThreads)
     yee_step_kernel(const StepArgs a) {
   extern __shared__ float smem[];
@@ -237,42 +225,6 @@ __global__ void __launch_bounds__(kMaxThreads)
         const float r = ffma(-s, e_old[c], cur[c]);
         e_new[c] = ffma(a.cb[c * N + i], r, e_old[c]);
         a.fout[c * N + i] = e_new[c];
-      }
-
-      if (REC == kRecSnap || REC == kRecProj) {
-        const int qx = x - a.ox, qy = y - a.oy, qz = z - a.oz;
-        if (qx >= 0 && qx < a.rx && qy >= 0 && qy < a.ry && qz >= 0 && qz < a.rz) {
-          const long long R = (long long)a.rx * a.ry * a.rz;
-          const long long ri = ((long long)qx * a.ry + qy) * a.rz + qz;
-          const float hnew[3] = {hx, hy, hz};
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            if (REC == kRecSnap) {
-              a.out[c * R + ri] = e_new[c];
-              if (a.record_h) a.out_h[c * R + ri] = hnew[c];
-            } else {
-              for (int r = 0; r < a.rows; ++r) {
-                const long long ai = ((long long)r * 3 + c) * R + ri;
-                kahan(&a.out[ai], &a.comp[ai], a.w[r], e_new[c]);
-                if (a.record_h) kahan(&a.out_h[ai], &a.comp_h[ai], a.w[r], hnew[c]);
-              }
-            }
-          }
-        }
-      }
-      if (REC == kRecGrad) {
-        const int gx = x - a.gx0, gy = y - a.gy0, gz = z - a.gz0;
-        if (gx >= 0 && gx < a.gnx && gy >= 0 && gy < a.gny && gz >= 0 && gz < a.gnz) {
-          const long long G = (long long)a.gnx * a.gny * a.gnz;
-          const long long g = ((long long)gx * a.gny + gy) * a.gnz + gz;
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            float coef = 0.f;
-            for (int r = 0; r < a.rows; ++r)
-              coef = ffma(a.w[r], a.q[((long long)r * 3 + c) * G + g], coef);
-            kahan(&a.out[c * G + g], &a.comp[c * G + g], coef, e_new[c]);
-          }
-        }
       }
     }
     hyp = hy;

@@ -187,7 +187,6 @@ __device__ __forceinline__ void compute_sync(int nthreads) {
 //   done[s]  -- every compute warp finished the plane in slot s, whose
 //               results sit in output buffer b = (x - x0) & 1 (count = warps);
 //   free[b]  -- the producer's bulk stores finished reading buffer b.
-template <int REC>
 __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) float sm[];
   const StepArgs& a = sa.s;
@@ -506,41 +505,6 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
           for (int c = 0; c < 3; ++c) {
             const float rr = ffma(-sig[c], eo[c][q], cur[c]);
             enew[c][q] = ffma(cbs[c][q], rr, eo[c][q]);
-          }
-          if (REC == kRecSnap || REC == kRecProj) {
-            const int qx = x - a.ox, qy = y - a.oy, qz = z - a.oz;
-            if (qx >= 0 && qx < a.rx && qy >= 0 && qy < a.ry && qz >= 0 && qz < a.rz) {
-              const long long R = (long long)a.rx * a.ry * a.rz;
-              const long long ri = ((long long)qx * a.ry + qy) * a.rz + qz;
-              const float hs3[3] = {hxs[q], hys[q], hzs[q]};
-#pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                if (REC == kRecSnap) {
-                  a.out[c * R + ri] = enew[c][q];
-                  if (a.record_h) a.out_h[c * R + ri] = hs3[c];
-                } else {
-                  for (int w = 0; w < a.rows; ++w) {
-                    const long long ai = ((long long)w * 3 + c) * R + ri;
-                    kahan(&a.out[ai], &a.comp[ai], a.w[w], enew[c][q]);
-                    if (a.record_h) kahan(&a.out_h[ai], &a.comp_h[ai], a.w[w], hs3[c]);
-                  }
-                }
-              }
-            }
-          }
-          if (REC == kRecGrad) {
-            const int gx = x - a.gx0, gy = y - a.gy0, gz = z - a.gz0;
-            if (gx >= 0 && gx < a.gnx && gy >= 0 && gy < a.gny && gz >= 0 && gz < a.gnz) {
-              const long long G = (long long)a.gnx * a.gny * a.gnz;
-              const long long gi = ((long long)gx * a.gny + gy) * a.gnz + gz;
-#pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                float coef = 0.f;
-                for (int w = 0; w < a.rows; ++w)
-                  coef = ffma(a.w[w], a.q[((long long)w * 3 + c) * G + gi], coef);
-                kahan(&a.out[c * G + gi], &a.comp[c * G + gi], coef, enew[c][q]);
-              }
-            }
           }
         }
 #pragma unroll
