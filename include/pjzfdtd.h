@@ -151,6 +151,24 @@ int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
                           void* workspace, size_t workspace_bytes,
                           int32_t step_begin, int32_t step_end, void* stream);
 
+/* Forward solve without any device allocation by anyone: the scratch is a
+   fixed 64 MiB array inside this library instead of a caller workspace.
+   No counterpart in the reference (pjz/fdtdz receive scratch from XLA).
+   For callers that cannot call cudaMalloc: a host whose device memory is
+   owned by another runtime's pool (for example an XLA custom call that was
+   given no scratch operand), or a real-time loop that must not risk the
+   implicit device synchronisation cudaMalloc/cudaFree can cause.  Plans
+   whose workspace (pjzfdtd_plan_workspace_bytes) exceeds 64 MiB are
+   rejected with PJZFDTD_ERR_WORKSPACE.  The first call on a device resolves
+   the array's device address (cudaGetSymbolAddress) with that device
+   current; make that first call before any stream capture.  All calls on a
+   device share the one array and it keeps the last call's contents (each
+   solve re-initialises what it needs); calls that overlap on the GPU, for
+   example on two streams, race on it.  Otherwise it behaves as
+   pjzfdtd_forward (same plan, buffers and results). */
+int32_t pjzfdtd_forward_static(pjzfdtd_plan* plan,
+                               const pjzfdtd_buffers* buffers, void* stream);
+
 /* Reads (and clears) the device status word of `workspace` after the work
    queued on `stream` so far: PJZFDTD_ERR_TIMEOUT if a bounded device-side
    wait gave up, PJZFDTD_OK otherwise.  Synchronises `stream`. */

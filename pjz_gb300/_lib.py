@@ -57,6 +57,7 @@ SIGNATURES = {
                                ctypes.c_size_t, _I, _I, _P]),
     "pjzfdtd_plan_launch_config": (_I, [_P] + [ctypes.POINTER(_I)] * 6),
     "pjzfdtd_plan_status": (_I, [_P, _P, ctypes.c_size_t, _P]),
+    "pjzfdtd_forward_static": (_I, [_P, ctypes.POINTER(Buffers), _P]),
 }
 
 _lib = None

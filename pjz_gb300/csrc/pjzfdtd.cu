@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -609,6 +610,56 @@ int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
   if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
   return run_range(plan, buffers, workspace, workspace_bytes, step_begin,
                    step_end, static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
+
+// Scratch for pjzfdtd_forward_static: a fixed device array, so a caller
+// that may not allocate device memory can still run a forward solve.  Every
+// GPU that loads this library holds it until the process exits.  All calls
+// on a device share it and it keeps the last call's contents; the forward
+// solve clears what must start at zero (fields, PML state, accumulators,
+// status word) at its first step.
+namespace {
+constexpr size_t kStaticScratchBytes = size_t(64) << 20;  // 64 MiB
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mu;
+void* g_static_ptr[kMaxDevices] = {};
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+extern "C" {
+
+int32_t pjzfdtd_forward_static(pjzfdtd_plan* plan,
+                               const pjzfdtd_buffers* buffers, void* stream) {
+  if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
+  if (plan->p.out_mode == PJZFDTD_OUT_GRADIENT)
+    return fail(PJZFDTD_ERR_INVALID, "GRADIENT plans run through pjzfdtd_adjoint");
+  if (plan->bytes > kStaticScratchBytes)
+    return fail(PJZFDTD_ERR_WORKSPACE,
+                "this plan needs %zu bytes of scratch; pjzfdtd_forward_static "
+                "has a fixed %zu-byte (64 MiB) array -- use pjzfdtd_forward "
+                "with a caller-allocated workspace",
+                plan->bytes, kStaticScratchBytes);
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(PJZFDTD_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+  void* scratch = nullptr;
+  {
+    // Once per device, with that device current: the host cannot use the
+    // array's symbol as a device address, so resolve the real one.
+    std::lock_guard<std::mutex> lock(g_static_mu);
+    if (!g_static_ptr[dev]) {
+      void* p = nullptr;
+      CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+      g_static_ptr[dev] = p;
+    }
+    scratch = g_static_ptr[dev];
+  }
+  return run_range(plan, buffers, scratch, kStaticScratchBytes, 0, plan->p.tt,
+                   static_cast<cudaStream_t>(stream));
 }
 
 }  // extern "C"
