@@ -151,6 +151,38 @@ int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
                           void* workspace, size_t workspace_bytes,
                           int32_t step_begin, int32_t step_end, void* stream);
 
+/* Replaces the recorded region of a SNAPSHOTS or PHASORS plan by `n` boxes
+   `boxes[6k..6k+5] = (x0, y0, z0, nx, ny, nz)` (domain cells).  `out` then
+   holds the boxes one after another, each shaped like a single-region output
+   ((ns,3,box) or (rows,3,box)); pjzfdtd_plan_output_floats gives the total.
+   Lets a caller keep phasors only where it needs them (a design region and
+   port planes) instead of the whole epsilon region. */
+int32_t pjzfdtd_plan_set_monitors(pjzfdtd_plan* plan, int32_t n,
+                                  const int32_t* boxes);
+
+/* Number of floats of `out` (and of `out_h`) the plan writes. */
+int32_t pjzfdtd_plan_output_floats(const pjzfdtd_plan* plan, size_t* floats);
+
+/* Batches independent problems (uneven domains, sources, frequencies, step
+   counts): every time step advances all of them in one launch of the
+   streamed kernel, whose blocks index a work table of (problem, tile,
+   segment); record passes follow at each problem's sample steps.  With
+   use_graph, the whole run is captured once into a CUDA graph and replayed
+   while the buffers and workspace stay the same (stream must not be the
+   legacy default stream).  This is the batched scheduler for many forward
+   and adjoint solves (multi-port S-matrices); pjz runs them as a Python loop
+   of `field` calls (src/pjz/_field.py:354-356).  Plans must be streamed
+   (zz % 4 == 0) and outlive the batch. */
+typedef struct pjzfdtd_batch pjzfdtd_batch;
+int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
+                             pjzfdtd_batch** batch);
+int32_t pjzfdtd_batch_workspace_bytes(const pjzfdtd_batch* batch, size_t* bytes);
+/* buffers: one pjzfdtd_buffers per plan, in plan order. */
+int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
+                          void* workspace, size_t workspace_bytes,
+                          int32_t use_graph, void* stream);
+int32_t pjzfdtd_batch_destroy(pjzfdtd_batch* batch);
+
 /* Forward solve without any device allocation by anyone: the scratch is a
    fixed 64 MiB array inside this library instead of a caller workspace.
    No counterpart in the reference (pjz/fdtdz receive scratch from XLA).

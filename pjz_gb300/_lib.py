@@ -58,6 +58,12 @@ SIGNATURES = {
     "pjzfdtd_plan_launch_config": (_I, [_P] + [ctypes.POINTER(_I)] * 6),
     "pjzfdtd_plan_status": (_I, [_P, _P, ctypes.c_size_t, _P]),
     "pjzfdtd_forward_static": (_I, [_P, ctypes.POINTER(Buffers), _P]),
+    "pjzfdtd_plan_set_monitors": (_I, [_P, _I, _P]),
+    "pjzfdtd_plan_output_floats": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "pjzfdtd_batch_create": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "pjzfdtd_batch_workspace_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "pjzfdtd_batch_run": (_I, [_P, _P, _P, ctypes.c_size_t, _I, _P]),
+    "pjzfdtd_batch_destroy": (_I, [_P]),
 }
 
 _lib = None

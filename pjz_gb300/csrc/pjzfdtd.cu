@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -59,6 +60,10 @@ struct pjzfdtd_plan {
   int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed
   int stages = 0;   // streamed ring depth
   size_t smem = 0;  // dynamic shared memory per CTA
+  // Recorded boxes (x0, y0, z0, nx, ny, nz) and their offsets in `out`.
+  std::vector<std::array<int32_t, 6>> boxes;
+  std::vector<size_t> box_off;
+  size_t out_floats = 0;
   // Workspace layout (byte offsets).
   size_t off_fa = 0, off_fb = 0, off_cb = 0, off_pa = 0, off_pb = 0,
          off_zc = 0, off_comp = 0, off_comph = 0, off_status = 0, off_mask = 0,
@@ -206,14 +211,37 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   return PJZFDTD_OK;
 }
 
+// Recorded boxes: the region (or the gradient box) unless monitors were set.
+// `out` holds the boxes one after another, each shaped like a single-region
+// output ((ns,3,box) snapshots, (rows,3,box) phasors, (3,box) gradient).
+void set_boxes(pjzfdtd_plan* pl) {
+  const pjzfdtd_problem& p = pl->p;
+  if (pl->boxes.empty()) {
+    if (p.out_mode == PJZFDTD_OUT_GRADIENT)
+      pl->boxes.push_back({p.grad_x0, p.grad_y0, p.grad_z0, p.grad_nx, p.grad_ny,
+                           p.grad_nz});
+    else if (p.out_mode != PJZFDTD_OUT_NONE)
+      pl->boxes.push_back({p.ox, p.oy, p.oz, p.rx, p.ry, p.rz});
+  }
+  const size_t per = p.out_mode == PJZFDTD_OUT_SNAPSHOTS ? (size_t)pl->ns * 3
+                     : p.out_mode == PJZFDTD_OUT_PHASORS ? (size_t)p.out_rows * 3
+                                                         : 3;
+  pl->box_off.clear();
+  size_t o = 0;
+  for (const auto& bx : pl->boxes) {
+    pl->box_off.push_back(o);
+    o += per * (size_t)bx[3] * bx[4] * bx[5];
+  }
+  pl->out_floats = o;
+}
+
 void layout(pjzfdtd_plan* pl) {
   const pjzfdtd_problem& p = pl->p;
   const size_t N = (size_t)pl->N;
   pl->Pp = round4(pl->P);
   pl->Yp = round4(p.yy);
+  set_boxes(pl);
   const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
-  const size_t R = (size_t)p.rx * p.ry * p.rz;
-  const size_t G = (size_t)p.grad_nx * p.grad_ny * p.grad_nz;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
@@ -226,9 +254,8 @@ void layout(pjzfdtd_plan* pl) {
   pl->off_pa = take(4 * XYP * sizeof(float));
   pl->off_pb = take(4 * XYP * sizeof(float));
   pl->off_zc = take(6 * (size_t)p.zz * sizeof(float));
-  size_t comp = 0;
-  if (p.out_mode == PJZFDTD_OUT_PHASORS) comp = (size_t)p.out_rows * 3 * R;
-  if (p.out_mode == PJZFDTD_OUT_GRADIENT) comp = 3 * G;
+  const size_t comp = (p.out_mode == PJZFDTD_OUT_PHASORS ||
+                       p.out_mode == PJZFDTD_OUT_GRADIENT) ? pl->out_floats : 0;
   pl->off_comp = take(std::max<size_t>(comp, 1) * sizeof(float));
   pl->off_comph = take(std::max<size_t>(p.record_h ? comp : 0, 1) * sizeof(float));
   pl->off_status = take(sizeof(int));
@@ -296,6 +323,181 @@ int32_t check_buffers(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b,
   return PJZFDTD_OK;
 }
 
+// Device pointers of one plan's workspace.
+struct RunPtrs {
+  float *fa, *fb, *cb, *pa, *pb, *zc, *comp, *comph, *mask_ws;
+  int* status;
+  RunPtrs(const pjzfdtd_plan* pl, void* ws)
+      : fa(at<float>(ws, pl->off_fa)), fb(at<float>(ws, pl->off_fb)),
+        cb(at<float>(ws, pl->off_cb)), pa(at<float>(ws, pl->off_pa)),
+        pb(at<float>(ws, pl->off_pb)), zc(at<float>(ws, pl->off_zc)),
+        comp(at<float>(ws, pl->off_comp)), comph(at<float>(ws, pl->off_comph)),
+        mask_ws(at<float>(ws, pl->off_mask)), status(at<int>(ws, pl->off_status)) {}
+};
+
+// Start-of-run work (stream-ordered, capturable unless copy_zc): zero the
+// state, outputs and status word, load the initial fields, build the
+// coefficient and absorber arrays.  The CPML table is a pageable host copy,
+// done here only when copy_zc.
+int32_t run_init(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
+                 cudaStream_t st, bool copy_zc) {
+  const pjzfdtd_problem& p = pl->p;
+  const long long N = pl->N;
+  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
+  RunPtrs w(pl, ws);
+  if (p.out_mode != PJZFDTD_OUT_NONE) {
+    // Snapshots before step 0 are zero; accumulators start at zero.
+    CUDA_TRY(cudaMemsetAsync(b->out, 0, pl->out_floats * sizeof(float), st));
+    if (p.record_h)
+      CUDA_TRY(cudaMemsetAsync(b->out_h, 0, pl->out_floats * sizeof(float), st));
+  }
+  if (p.out_mode == PJZFDTD_OUT_PHASORS || p.out_mode == PJZFDTD_OUT_GRADIENT) {
+    CUDA_TRY(cudaMemsetAsync(w.comp, 0, pl->out_floats * sizeof(float), st));
+    if (p.record_h)
+      CUDA_TRY(cudaMemsetAsync(w.comph, 0, pl->out_floats * sizeof(float), st));
+  }
+  if (copy_zc)
+    CUDA_TRY(cudaMemcpyAsync(w.zc, pl->zc.data(), pl->zc.size() * sizeof(float),
+                             cudaMemcpyHostToDevice, st));
+  if (b->fields)
+    CUDA_TRY(cudaMemcpyAsync(w.fa, b->fields, 6 * N * sizeof(float),
+                             cudaMemcpyDeviceToDevice, st));
+  else
+    CUDA_TRY(cudaMemsetAsync(w.fa, 0, 6 * N * sizeof(float), st));
+  CUDA_TRY(cudaMemsetAsync(w.pa, 0, 4 * XYP * sizeof(float), st));
+  CUDA_TRY(cudaMemsetAsync(w.pb, 0, 4 * XYP * sizeof(float), st));
+  CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+  const int threads = 256;
+  const long long total = 3 * N;
+  const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 1 << 20);
+  precompute_cb_kernel<<<blocks, threads, 0, st>>>(
+      b->epsilon, b->absorption_mask, w.cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
+      p.rx, p.ry, p.rz, p.dt);
+  CUDA_TRY(cudaGetLastError());
+  if (pl->kernel == 2) {
+    const long long nm = (long long)p.xx * 3 * pl->Yp;
+    pad_mask_kernel<<<(int)std::min<long long>((nm + 255) / 256, 1 << 16), 256, 0,
+                      st>>>(b->absorption_mask, w.mask_ws, p.xx, p.yy, pl->Yp);
+    CUDA_TRY(cudaGetLastError());
+  }
+  return PJZFDTD_OK;
+}
+
+// Step arguments of step n (ping-pong parity and waveform row).
+StepArgs step_args(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
+                   int n) {
+  const pjzfdtd_problem& p = pl->p;
+  RunPtrs w(pl, ws);
+  StepArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.X = p.xx;
+  a.Y = p.yy;
+  a.Z = p.zz;
+  a.P = pl->P;
+  a.Pst = std::max(pl->Pp, 1);
+  a.plo = p.pml_lo;
+  a.phi = p.pml_hi;
+  a.N = pl->N;
+  a.dt = p.dt;
+  a.tile_y = pl->tile_y;
+  a.seg_x = pl->seg_x;
+  a.cb = w.cb;
+  a.mask = b->absorption_mask;
+  a.zc = w.zc;
+  a.sx0 = p.src_x0;
+  a.sy0 = p.src_y0;
+  a.sz0 = p.src_z0;
+  a.snx = p.src_ncols > 0 ? p.src_nx : 0;
+  a.sny = p.src_ncols > 0 ? p.src_ny : 0;
+  a.snz = p.src_ncols > 0 ? p.src_nz : 0;
+  a.snc = p.src_ncols;
+  a.src = b->source;
+  const bool even = (n % 2) == 0;
+  a.fin = even ? w.fa : w.fb;
+  a.fout = even ? w.fb : w.fa;
+  a.psi_in = even ? w.pa : w.pb;
+  a.psi_out = even ? w.pb : w.pa;
+  a.wave = p.src_ncols > 0 ? b->waveform + (size_t)n * p.src_ncols : nullptr;
+  return a;
+}
+
+StreamArgs stream_args(const pjzfdtd_plan* pl, void* ws, const StepArgs& a) {
+  RunPtrs w(pl, ws);
+  StreamArgs sa;
+  std::memset(&sa, 0, sizeof(sa));
+  sa.s = a;
+  sa.stages = pl->stages;
+  sa.status = w.status;
+  sa.Yp = pl->Yp;
+  sa.mask_ws = w.mask_ws;
+  return sa;
+}
+
+bool is_sample(const pjzfdtd_problem& p, int n) {
+  return p.out_mode != PJZFDTD_OUT_NONE && n >= p.out_start && n < p.out_stop &&
+         (n - p.out_start) % p.out_step == 0;
+}
+
+// Record pass of step n (a sample step) over every box, from state `f`.
+int32_t record_step(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
+                    int n, const float* f, cudaStream_t st) {
+  const pjzfdtd_problem& p = pl->p;
+  RunPtrs w(pl, ws);
+  const int j = (n - p.out_start) / p.out_step;
+  RecordArgs ra;
+  std::memset(&ra, 0, sizeof(ra));
+  ra.f = f;
+  ra.N = pl->N;
+  ra.X = p.xx;
+  ra.Y = p.yy;
+  ra.Z = p.zz;
+  ra.record_h = p.record_h;
+  ra.rows = p.out_rows;
+  ra.q = b->q;
+  if (p.out_mode != PJZFDTD_OUT_SNAPSHOTS)
+    for (int r = 0; r < p.out_rows; ++r) ra.w[r] = pl->weights[(size_t)r * pl->ns + j];
+  for (size_t k = 0; k < pl->boxes.size(); ++k) {
+    const auto& bx = pl->boxes[k];
+    ra.bx0 = bx[0];
+    ra.by0 = bx[1];
+    ra.bz0 = bx[2];
+    ra.bnx = bx[3];
+    ra.bny = bx[4];
+    ra.bnz = bx[5];
+    const long long nb = (long long)bx[3] * bx[4] * bx[5];
+    size_t o = pl->box_off[k];
+    if (p.out_mode == PJZFDTD_OUT_SNAPSHOTS) o += (size_t)j * 3 * nb;
+    ra.out = b->out + o;
+    ra.out_h = p.record_h ? b->out_h + o : nullptr;
+    ra.comp = w.comp + pl->box_off[k];
+    ra.comp_h = w.comph + pl->box_off[k];
+    const int rblocks = (int)std::min<long long>((nb + 255) / 256, 1 << 20);
+    switch (p.out_mode) {
+      case PJZFDTD_OUT_SNAPSHOTS:
+        record_kernel<kRecSnap><<<rblocks, 256, 0, st>>>(ra);
+        break;
+      case PJZFDTD_OUT_PHASORS:
+        record_kernel<kRecProj><<<rblocks, 256, 0, st>>>(ra);
+        break;
+      default:
+        record_kernel<kRecGrad><<<rblocks, 256, 0, st>>>(ra);
+        break;
+    }
+    CUDA_TRY(cudaGetLastError());
+  }
+  return PJZFDTD_OK;
+}
+
+int32_t run_finish(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
+                   cudaStream_t st) {
+  if (!b->fields) return PJZFDTD_OK;
+  RunPtrs w(pl, ws);
+  float* fin = (pl->p.tt % 2 == 0) ? w.fa : w.fb;
+  CUDA_TRY(cudaMemcpyAsync(b->fields, fin, 6 * pl->N * sizeof(float),
+                           cudaMemcpyDeviceToDevice, st));
+  return PJZFDTD_OK;
+}
+
 int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
                   size_t ws_bytes, int n0, int n1, cudaStream_t st) {
   int32_t rc = check_buffers(pl, b, ws, ws_bytes);
@@ -306,165 +508,78 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   rc = resolve_seg_x(pl);
   if (rc) return rc;
   const pjzfdtd_problem& p = pl->p;
-  const long long N = pl->N;
-  const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
-  float* fa = at<float>(ws, pl->off_fa);
-  float* fb = at<float>(ws, pl->off_fb);
-  float* cb = at<float>(ws, pl->off_cb);
-  float* pa = at<float>(ws, pl->off_pa);
-  float* pb = at<float>(ws, pl->off_pb);
-  float* zc = at<float>(ws, pl->off_zc);
-  float* comp = at<float>(ws, pl->off_comp);
-  float* comph = at<float>(ws, pl->off_comph);
-  const size_t R = (size_t)p.rx * p.ry * p.rz;
-  const size_t G = (size_t)p.grad_nx * p.grad_ny * p.grad_nz;
-
-  if (n0 == 0) {
-    if (p.out_mode == PJZFDTD_OUT_SNAPSHOTS && p.out_start < 0) {
-      const size_t n = (size_t)pl->ns * 3 * R * sizeof(float);
-      CUDA_TRY(cudaMemsetAsync(b->out, 0, n, st));
-      if (p.record_h) CUDA_TRY(cudaMemsetAsync(b->out_h, 0, n, st));
-    }
-    CUDA_TRY(cudaMemcpyAsync(zc, pl->zc.data(), pl->zc.size() * sizeof(float),
-                             cudaMemcpyHostToDevice, st));
-    if (b->fields)
-      CUDA_TRY(cudaMemcpyAsync(fa, b->fields, 6 * N * sizeof(float),
-                               cudaMemcpyDeviceToDevice, st));
-    else
-      CUDA_TRY(cudaMemsetAsync(fa, 0, 6 * N * sizeof(float), st));
-    CUDA_TRY(cudaMemsetAsync(pa, 0, 4 * XYP * sizeof(float), st));
-    CUDA_TRY(cudaMemsetAsync(pb, 0, 4 * XYP * sizeof(float), st));
-    if (p.out_mode == PJZFDTD_OUT_PHASORS) {
-      const size_t n = (size_t)p.out_rows * 3 * R * sizeof(float);
-      CUDA_TRY(cudaMemsetAsync(b->out, 0, n, st));
-      CUDA_TRY(cudaMemsetAsync(comp, 0, n, st));
-      if (p.record_h) {
-        CUDA_TRY(cudaMemsetAsync(b->out_h, 0, n, st));
-        CUDA_TRY(cudaMemsetAsync(comph, 0, n, st));
-      }
-    }
-    if (p.out_mode == PJZFDTD_OUT_GRADIENT) {
-      CUDA_TRY(cudaMemsetAsync(b->out, 0, 3 * G * sizeof(float), st));
-      CUDA_TRY(cudaMemsetAsync(comp, 0, 3 * G * sizeof(float), st));
-    }
-    const int threads = 256;
-    const long long total = 3 * N;
-    const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 1 << 20);
-    precompute_cb_kernel<<<blocks, threads, 0, st>>>(
-        b->epsilon, b->absorption_mask, cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
-        p.rx, p.ry, p.rz, p.dt);
-    CUDA_TRY(cudaGetLastError());
-    if (pl->kernel == 2) {
-      const long long nm = (long long)p.xx * 3 * pl->Yp;
-      pad_mask_kernel<<<(int)std::min<long long>((nm + 255) / 256, 1 << 16), 256, 0,
-                        st>>>(b->absorption_mask, at<float>(ws, pl->off_mask),
-                              p.xx, p.yy, pl->Yp);
-      CUDA_TRY(cudaGetLastError());
-    }
-  }
-
-  StepArgs a;
-  std::memset(&a, 0, sizeof(a));
-  a.X = p.xx;
-  a.Y = p.yy;
-  a.Z = p.zz;
-  a.P = pl->P;
-  a.Pst = std::max(pl->Pp, 1);
-  a.plo = p.pml_lo;
-  a.phi = p.pml_hi;
-  a.N = N;
-  a.dt = p.dt;
-  a.tile_y = pl->tile_y;
-  a.seg_x = pl->seg_x;
-  a.cb = cb;
-  a.mask = b->absorption_mask;
-  a.zc = zc;
-  a.sx0 = p.src_x0;
-  a.sy0 = p.src_y0;
-  a.sz0 = p.src_z0;
-  a.snx = p.src_ncols > 0 ? p.src_nx : 0;
-  a.sny = p.src_ncols > 0 ? p.src_ny : 0;
-  a.snz = p.src_ncols > 0 ? p.src_nz : 0;
-  a.snc = p.src_ncols;
-  a.src = b->source;
-
+  if (n0 == 0 && (rc = run_init(pl, b, ws, st, true))) return rc;
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
-  const size_t smem = pl->smem;
-  int* status = at<int>(ws, pl->off_status);
-  if (n0 == 0) CUDA_TRY(cudaMemsetAsync(status, 0, sizeof(int), st));
-  if (pl->kernel == 2) CUDA_TRY(set_stream_smem(smem));
-  RecordArgs ra;
-  std::memset(&ra, 0, sizeof(ra));
-  ra.N = N;
-  ra.X = p.xx;
-  ra.Y = p.yy;
-  ra.Z = p.zz;
-  if (p.out_mode == PJZFDTD_OUT_GRADIENT) {
-    ra.bx0 = p.grad_x0; ra.by0 = p.grad_y0; ra.bz0 = p.grad_z0;
-    ra.bnx = p.grad_nx; ra.bny = p.grad_ny; ra.bnz = p.grad_nz;
-  } else {
-    ra.bx0 = p.ox; ra.by0 = p.oy; ra.bz0 = p.oz;
-    ra.bnx = p.rx; ra.bny = p.ry; ra.bnz = p.rz;
-  }
-  ra.record_h = p.record_h;
-  ra.out = b->out;
-  ra.out_h = b->out_h;
-  ra.comp = comp;
-  ra.comp_h = comph;
-  ra.rows = p.out_rows;
-  ra.q = b->q;
-  StreamArgs sa;
-  sa.stages = pl->stages;
-  sa.status = status;
-  sa.Yp = pl->Yp;
-  sa.mask_ws = at<float>(ws, pl->off_mask);
+  if (pl->kernel == 2) CUDA_TRY(set_stream_smem(pl->smem));
   for (int n = n0; n < n1; ++n) {
-    const bool even = (n % 2) == 0;
-    a.fin = even ? fa : fb;
-    a.fout = even ? fb : fa;
-    a.psi_in = even ? pa : pb;
-    a.psi_out = even ? pb : pa;
-    a.wave = p.src_ncols > 0 ? b->waveform + (size_t)n * p.src_ncols : nullptr;
-    if (pl->kernel == 2) {
-      sa.s = a;
-      yee_stream_kernel<<<grid, pl->threads, smem, st>>>(sa);
-    } else {
-      yee_step_kernel<<<grid, pl->threads, smem, st>>>(a);
-    }
+    const StepArgs a = step_args(pl, b, ws, n);
+    if (pl->kernel == 2)
+      yee_stream_kernel<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
+    else
+      yee_step_kernel<<<grid, pl->threads, pl->smem, st>>>(a);
     CUDA_TRY(cudaGetLastError());
-    if (p.out_mode != PJZFDTD_OUT_NONE && n >= p.out_start && n < p.out_stop &&
-        (n - p.out_start) % p.out_step == 0) {
-      const int j = (n - p.out_start) / p.out_step;
-      ra.f = a.fout;
-      if (p.out_mode == PJZFDTD_OUT_SNAPSHOTS) {
-        ra.out = b->out + (size_t)j * 3 * R;
-        ra.out_h = p.record_h ? b->out_h + (size_t)j * 3 * R : nullptr;
-      } else {
-        for (int r = 0; r < p.out_rows; ++r)
-          ra.w[r] = pl->weights[(size_t)r * pl->ns + j];
-      }
-      const long long nb = (long long)ra.bnx * ra.bny * ra.bnz;
-      const int rblocks = (int)std::min<long long>((nb + 255) / 256, 1 << 20);
-      switch (p.out_mode) {
-        case PJZFDTD_OUT_SNAPSHOTS:
-          record_kernel<kRecSnap><<<rblocks, 256, 0, st>>>(ra);
-          break;
-        case PJZFDTD_OUT_PHASORS:
-          record_kernel<kRecProj><<<rblocks, 256, 0, st>>>(ra);
-          break;
-        default:
-          record_kernel<kRecGrad><<<rblocks, 256, 0, st>>>(ra);
-          break;
-      }
+    if (is_sample(p, n) && (rc = record_step(pl, b, ws, n, a.fout, st))) return rc;
+  }
+  if (n1 == p.tt) return run_finish(pl, b, ws, st);
+  return PJZFDTD_OK;
+}
+
+}  // namespace
+
+struct pjzfdtd_batch {
+  std::vector<pjzfdtd_plan*> plans;
+  std::vector<size_t> off;  // workspace offset of each plan
+  size_t off_args = 0, off_work = 0, bytes = 0;
+  int max_work = 0;
+  int tt_max = 0;
+  size_t smem = 0;
+  // Cached CUDA graph of a whole run and the buffers it was captured with.
+  cudaGraphExec_t exec = nullptr;
+  std::vector<pjzfdtd_buffers> gbufs;
+  void* gws = nullptr;
+  cudaStream_t gstream = nullptr;
+  ~pjzfdtd_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+namespace {
+
+bool same_buffers(const pjzfdtd_buffers& a, const pjzfdtd_buffers& b) {
+  return std::memcmp(&a, &b, sizeof(a)) == 0;
+}
+
+// Enqueues one whole batched run on `st` (capturable: no host copies).
+int32_t batch_enqueue(pjzfdtd_batch* bt, const pjzfdtd_buffers* bufs, void* ws,
+                      const std::vector<int>& active, cudaStream_t st) {
+  const int n = (int)bt->plans.size();
+  int32_t rc;
+  for (int i = 0; i < n; ++i)
+    if ((rc = run_init(bt->plans[i], &bufs[i], at<char>(ws, bt->off[i]), st, false)))
+      return rc;
+  BatchArgs ba;
+  ba.args = at<const StreamArgs>(ws, bt->off_args);
+  ba.work = at<const int4>(ws, bt->off_work);
+  ba.nsim = n;
+  for (int step = 0; step < bt->tt_max; ++step) {
+    ba.step = step;
+    if (active[step] > 0) {
+      yee_stream_batch_kernel<<<active[step], kStreamThreads, bt->smem, st>>>(ba);
       CUDA_TRY(cudaGetLastError());
     }
+    for (int i = 0; i < n; ++i) {
+      const pjzfdtd_plan* pl = bt->plans[i];
+      if (step >= pl->p.tt || !is_sample(pl->p, step)) continue;
+      void* wsi = at<char>(ws, bt->off[i]);
+      RunPtrs w(pl, wsi);
+      const float* fout = (step % 2 == 0) ? w.fb : w.fa;
+      if ((rc = record_step(pl, &bufs[i], wsi, step, fout, st))) return rc;
+    }
   }
-  if (n1 == p.tt && b->fields) {
-    float* fin = (p.tt % 2 == 0) ? fa : fb;
-    CUDA_TRY(cudaMemcpyAsync(b->fields, fin, 6 * N * sizeof(float),
-                             cudaMemcpyDeviceToDevice, st));
-  }
+  for (int i = 0; i < n; ++i)
+    if ((rc = run_finish(bt->plans[i], &bufs[i], at<char>(ws, bt->off[i]), st)))
+      return rc;
   return PJZFDTD_OK;
 }
 
@@ -610,6 +725,186 @@ int32_t pjzfdtd_run_steps(pjzfdtd_plan* plan, const pjzfdtd_buffers* buffers,
   if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
   return run_range(plan, buffers, workspace, workspace_bytes, step_begin,
                    step_end, static_cast<cudaStream_t>(stream));
+}
+
+int32_t pjzfdtd_plan_set_monitors(pjzfdtd_plan* plan, int32_t n,
+                                  const int32_t* boxes) {
+  if (!plan || n < 1 || !boxes)
+    return fail(PJZFDTD_ERR_INVALID, "need a plan and at least one box");
+  const pjzfdtd_problem& p = plan->p;
+  if (p.out_mode != PJZFDTD_OUT_SNAPSHOTS && p.out_mode != PJZFDTD_OUT_PHASORS)
+    return fail(PJZFDTD_ERR_INVALID, "monitors apply to SNAPSHOTS and PHASORS plans");
+  std::vector<std::array<int32_t, 6>> v;
+  for (int k = 0; k < n; ++k) {
+    const int32_t* b = boxes + 6 * k;
+    if (b[0] < 0 || b[1] < 0 || b[2] < 0 || b[3] <= 0 || b[4] <= 0 || b[5] <= 0 ||
+        b[0] + b[3] > p.xx || b[1] + b[4] > p.yy || b[2] + b[5] > p.zz)
+      return fail(PJZFDTD_ERR_INVALID,
+                  "monitor %d (%d, %d, %d)+(%d, %d, %d) outside the domain", k,
+                  b[0], b[1], b[2], b[3], b[4], b[5]);
+    v.push_back({b[0], b[1], b[2], b[3], b[4], b[5]});
+  }
+  plan->boxes = v;
+  layout(plan);
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_plan_output_floats(const pjzfdtd_plan* plan, size_t* floats) {
+  if (!plan || !floats) return fail(PJZFDTD_ERR_INVALID, "NULL argument");
+  *floats = plan->out_floats;
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
+                             pjzfdtd_batch** batch) {
+  if (!plans || n < 1 || !batch)
+    return fail(PJZFDTD_ERR_INVALID, "need at least one plan");
+  *batch = nullptr;
+  pjzfdtd_batch* bt = new (std::nothrow) pjzfdtd_batch();
+  if (!bt) return fail(PJZFDTD_ERR_INVALID, "out of host memory");
+  size_t o = 0;
+  for (int i = 0; i < n; ++i) {
+    pjzfdtd_plan* pl = plans[i];
+    if (!pl || pl->kernel != 2) {
+      delete bt;
+      return fail(PJZFDTD_ERR_UNSUPPORTED,
+                  "plan %d is not a streamed-kernel plan (zz %% 4 == 0 needed)", i);
+    }
+    bt->plans.push_back(pl);
+    bt->off.push_back(o);
+    o = align256(o + pl->bytes);
+    bt->tt_max = std::max(bt->tt_max, pl->p.tt);
+    bt->smem = std::max(bt->smem, pl->smem);
+    // Segments are at least 8 planes long (or the whole x extent).
+    const int tiles = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
+    const int minseg = std::min(pl->p.xx, 8);
+    bt->max_work += tiles * ((pl->p.xx + minseg - 1) / minseg);
+  }
+  bt->off_args = o;
+  o = align256(o + 2 * (size_t)n * sizeof(StreamArgs));
+  bt->off_work = o;
+  o = align256(o + (size_t)bt->max_work * sizeof(int4));
+  bt->bytes = o;
+  *batch = bt;
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_batch_workspace_bytes(const pjzfdtd_batch* batch, size_t* bytes) {
+  if (!batch || !bytes) return fail(PJZFDTD_ERR_INVALID, "NULL argument");
+  *bytes = batch->bytes;
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
+                          void* workspace, size_t workspace_bytes,
+                          int32_t use_graph, void* stream) {
+  if (!batch || !buffers) return fail(PJZFDTD_ERR_INVALID, "NULL argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int n = (int)batch->plans.size();
+  if (!workspace || workspace_bytes < batch->bytes)
+    return fail(PJZFDTD_ERR_WORKSPACE, "batch workspace of %zu bytes needed",
+                batch->bytes);
+  if (reinterpret_cast<uintptr_t>(workspace) % 256)
+    return fail(PJZFDTD_ERR_WORKSPACE, "workspace must be 256-byte aligned");
+  if (use_graph && st == nullptr)
+    return fail(PJZFDTD_ERR_INVALID,
+                "graph capture needs a stream other than the legacy default");
+  int32_t rc;
+  for (int i = 0; i < n; ++i) {
+    pjzfdtd_plan* pl = batch->plans[i];
+    if ((rc = check_buffers(pl, &buffers[i], at<char>(workspace, batch->off[i]),
+                            pl->bytes)))
+      return rc;
+    if ((rc = resolve_seg_x(pl))) return rc;
+  }
+  if (use_graph && batch->exec && batch->gws == workspace && batch->gstream == st) {
+    bool same = true;
+    for (int i = 0; i < n && same; ++i)
+      same = same_buffers(batch->gbufs[i], buffers[i]);
+    if (same) {
+      CUDA_TRY(cudaGraphLaunch(batch->exec, st));
+      return PJZFDTD_OK;
+    }
+  }
+  // Work table, longest-running problems first so that the active entries of
+  // every step form a prefix; per-problem step arguments for both parities.
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return batch->plans[a]->p.tt > batch->plans[b]->p.tt;
+  });
+  std::vector<int4> work;
+  std::vector<int> prefix_end(n);
+  for (int r = 0; r < n; ++r) {
+    const pjzfdtd_plan* pl = batch->plans[order[r]];
+    const int tiles = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
+    const int segs = (pl->p.xx + pl->seg_x - 1) / pl->seg_x;
+    for (int t = 0; t < tiles; ++t)
+      for (int sg = 0; sg < segs; ++sg) work.push_back(make_int4(order[r], t, sg, 0));
+    prefix_end[r] = (int)work.size();
+  }
+  if ((int)work.size() > batch->max_work)
+    return fail(PJZFDTD_ERR_INVALID, "work table overflow");
+  std::vector<int> active(batch->tt_max, 0);
+  for (int step = 0; step < batch->tt_max; ++step)
+    for (int r = 0; r < n; ++r)
+      if (batch->plans[order[r]]->p.tt > step) active[step] = prefix_end[r];
+  std::vector<StreamArgs> args(2 * (size_t)n);
+  for (int parity = 0; parity < 2; ++parity)
+    for (int i = 0; i < n; ++i) {
+      void* wsi = at<char>(workspace, batch->off[i]);
+      StepArgs a = step_args(batch->plans[i], &buffers[i], wsi, parity);
+      a.wave = buffers[i].waveform;  // row 0; the kernel adds step * ncols
+      args[(size_t)parity * n + i] = stream_args(batch->plans[i], wsi, a);
+    }
+  // Host copies (not capturable from pageable memory) happen before capture.
+  CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, batch->off_args), args.data(),
+                           args.size() * sizeof(StreamArgs), cudaMemcpyHostToDevice,
+                           st));
+  CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, batch->off_work), work.data(),
+                           work.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+  for (int i = 0; i < n; ++i) {
+    pjzfdtd_plan* pl = batch->plans[i];
+    RunPtrs w(pl, at<char>(workspace, batch->off[i]));
+    CUDA_TRY(cudaMemcpyAsync(w.zc, pl->zc.data(), pl->zc.size() * sizeof(float),
+                             cudaMemcpyHostToDevice, st));
+  }
+  CUDA_TRY(cudaFuncSetAttribute(yee_stream_batch_kernel,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)batch->smem));
+  if (!use_graph) return batch_enqueue(batch, buffers, workspace, active, st);
+
+  CUDA_TRY(cudaStreamSynchronize(st));  // host copies above read pageable memory
+  if (batch->exec) {
+    cudaGraphExecDestroy(batch->exec);
+    batch->exec = nullptr;
+  }
+  CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+  rc = batch_enqueue(batch, buffers, workspace, active, st);
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (ec != cudaSuccess)
+    return fail(PJZFDTD_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ec));
+  const cudaError_t ei = cudaGraphInstantiate(&batch->exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) {
+    batch->exec = nullptr;
+    return fail(PJZFDTD_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+  }
+  batch->gbufs.assign(buffers, buffers + n);
+  batch->gws = workspace;
+  batch->gstream = st;
+  CUDA_TRY(cudaGraphLaunch(batch->exec, st));
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_batch_destroy(pjzfdtd_batch* batch) {
+  delete batch;
+  return PJZFDTD_OK;
 }
 
 }  // extern "C"

@@ -187,8 +187,10 @@ __device__ __forceinline__ void compute_sync(int nthreads) {
 //   done[s]  -- every compute warp finished the plane in slot s, whose
 //               results sit in output buffer b = (x - x0) & 1 (count = warps);
 //   free[b]  -- the producer's bulk stores finished reading buffer b.
-__global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
-  extern __shared__ __align__(16) float sm[];
+// One CTA's work: tile `tile` of y rows and segment `seg` of x planes of the
+// problem described by `sa`.
+__device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
+                                            int seg, float* sm) {
   const StepArgs& a = sa.s;
   const int X = a.X, Y = a.Y, Z = a.Z, TY = a.tile_y;
   const int S = sa.stages;
@@ -210,8 +212,8 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   const int rpt = ncomp / Zh;             // rows per pass
   const int z0 = 2 * (tid % Zh);
   const int rt = tid / Zh;                // >= rpt: idle compute thread
-  const int y0 = blockIdx.x * TY;
-  const int xs = blockIdx.y * a.seg_x;
+  const int y0 = tile * TY;
+  const int xs = seg * a.seg_x;
   const int xe = min(X, xs + a.seg_x);
   const int x0 = xs > 0 ? xs - 1 : 0;
   const int xlast = min(xe, X - 1);  // last plane whose E is read
@@ -521,6 +523,30 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
     // H(x-1) (hprev) is rewritten by the next plane's H phase.
     compute_sync(ncomp);
   }
+}
+
+__global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
+  extern __shared__ __align__(16) float sm[];
+  stream_tile(sa, blockIdx.x, blockIdx.y, sm);
+}
+
+// Several independent problems advanced by one step in one launch.  Block b
+// runs entry `work[b] = (sim, tile, seg)`; `args[parity][sim]` holds each
+// problem's step arguments for even / odd steps (ping-pong buffers) with the
+// waveform row pointer at step 0, offset here by the step index.
+struct BatchArgs {
+  const StreamArgs* __restrict__ args;  // [2][nsim]
+  const int4* __restrict__ work;        // [nwork]: sim, tile, seg, unused
+  int nsim;
+  int step;
+};
+
+__global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs ba) {
+  extern __shared__ __align__(16) float sm[];
+  const int4 w = ba.work[blockIdx.x];
+  StreamArgs sa = ba.args[(ba.step & 1) * ba.nsim + w.x];
+  if (sa.s.snc > 0) sa.s.wave += (long long)ba.step * sa.s.snc;
+  stream_tile(sa, w.y, w.z, sm);
 }
 
 // Absorber conductivity re-laid out as [x][c][Yp] (Yp % 4 == 0, zero tail)

@@ -59,7 +59,7 @@ class Plan:
                grad_origin: Tuple[int, int, int] = (0, 0, 0),
                grad_shape: Tuple[int, int, int] = (0, 0, 0),
                tile_y: int = 0, seg_x: int = 0, steps_per_pass: int = 0,
-               kernel: int = 0, stages: int = 0):
+               kernel: int = 0, stages: int = 0, monitors=None):
     lib = _lib.load()
     p = _lib.Problem()
     p.xx, p.yy, p.zz = (int(v) for v in domain)
@@ -107,6 +107,34 @@ class Plan:
     self._ws = None
     if w is not None and w.shape[1] != self.num_samples:
       raise ValueError(f"weights must have {self.num_samples} columns")
+    self.monitors = None
+    if monitors:
+      self.set_monitors(monitors)
+
+  def set_monitors(self, boxes):
+    """Records only ``boxes`` (list of (origin, shape) in domain cells);
+    ``out`` becomes flat, see :meth:`split`."""
+    arr = np.ascontiguousarray(
+        [[*map(int, o), *map(int, s)] for o, s in boxes], dtype=np.int32)
+    _lib.check(self._lib.pjzfdtd_plan_set_monitors(self._h, len(boxes),
+                                                   arr.ctypes.data))
+    self.monitors = [(tuple(map(int, o)), tuple(map(int, s))) for o, s in boxes]
+    nb = ctypes.c_size_t()
+    _lib.check(self._lib.pjzfdtd_plan_workspace_bytes(self._h, ctypes.byref(nb)))
+    self.workspace_bytes = nb.value
+    self._ws = None
+
+  def split(self, out: torch.Tensor):
+    """Per-monitor views of a flat ``out``: ``(lead, 3, nx, ny, nz)`` each,
+    ``lead`` = samples (snapshots) or weight rows (phasors)."""
+    p = self.problem
+    lead = self.num_samples if p.out_mode == OUT_SNAPSHOTS else p.out_rows
+    views, o = [], 0
+    for _, s in self.monitors:
+      n = lead * 3 * s[0] * s[1] * s[2]
+      views.append(out[o:o + n].view(lead, 3, *s))
+      o += n
+    return views
 
   def __del__(self):
     h = getattr(self, "_h", None)
@@ -127,6 +155,10 @@ class Plan:
 
   def out_shape(self):
     p = self.problem
+    if self.monitors:
+      n = ctypes.c_size_t()
+      _lib.check(self._lib.pjzfdtd_plan_output_floats(self._h, ctypes.byref(n)))
+      return (n.value,)
     if p.out_mode == OUT_SNAPSHOTS:
       return (self.num_samples, 3) + self.region
     if p.out_mode == OUT_PHASORS:
@@ -161,10 +193,10 @@ class Plan:
     return self._ws
 
   # -- execution ------------------------------------------------------------
-  def run(self, *, epsilon, absorption_mask, source=None, waveform=None,
-          q=None, out=None, out_h=None, fields=None, steps=None,
-          workspace: Optional[torch.Tensor] = None):
-    """Runs the plan; returns ``(out, out_h)`` (``out_h`` None unless H)."""
+  def buffers(self, *, epsilon, absorption_mask, source=None, waveform=None,
+              q=None, out=None, out_h=None, fields=None):
+    """Validates the device arrays of one run and allocates missing outputs;
+    returns ``(pjzfdtd_buffers, keep-alive tensors, out, out_h)``."""
     p = self.problem
     dev = epsilon.device if isinstance(epsilon, torch.Tensor) else torch.device("cuda")
     if dev.type != "cuda":
@@ -194,10 +226,22 @@ class Plan:
           or tuple(fields.shape) != (6,) + self.domain or fields.device != dev):
         raise ValueError(f"fields must be a contiguous float32 {(6,) + self.domain}"
                          f" tensor on {dev}")
-    ws = workspace if workspace is not None else self.workspace(dev)
     b = _lib.Buffers(epsilon=_ptr(eps), absorption_mask=_ptr(mask),
                      source=_ptr(src), waveform=_ptr(wave), q=_ptr(qq),
                      out=_ptr(out), out_h=_ptr(out_h), fields=_ptr(fields))
+    keep = (eps, mask, src, wave, qq, out, out_h, fields)
+    return b, keep, out, out_h
+
+  def run(self, *, epsilon, absorption_mask, source=None, waveform=None,
+          q=None, out=None, out_h=None, fields=None, steps=None,
+          workspace: Optional[torch.Tensor] = None):
+    """Runs the plan; returns ``(out, out_h)`` (``out_h`` None unless H)."""
+    p = self.problem
+    b, keep, out, out_h = self.buffers(
+        epsilon=epsilon, absorption_mask=absorption_mask, source=source,
+        waveform=waveform, q=q, out=out, out_h=out_h, fields=fields)
+    dev = keep[0].device
+    ws = workspace if workspace is not None else self.workspace(dev)
     with torch.cuda.device(dev):
       stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
       ws_ptr = ctypes.c_void_p(ws.data_ptr())
@@ -268,3 +312,78 @@ def plane_source_box(source_field: torch.Tensor, source_position: int,
   origin = [0, 0, 0]
   origin[axis] = lo
   return tuple(origin), tuple(shape), prof
+
+
+class Batch:
+  """Independent plans advanced together: one kernel launch per time step
+  for all of them, the whole run captured once into a CUDA graph.
+
+  ``run`` takes one dict of :meth:`Plan.run` arguments per plan and returns
+  the ``(out, out_h)`` pairs.  Graph replays need the same output tensors
+  and inputs each time, so pass ``out`` tensors to reuse a captured graph.
+  """
+
+  def __init__(self, plans):
+    lib = _lib.load()
+    self.plans = list(plans)
+    arr = (ctypes.c_void_p * len(self.plans))(*[p._h.value for p in self.plans])
+    h = ctypes.c_void_p()
+    _lib.check(lib.pjzfdtd_batch_create(arr, len(self.plans), ctypes.byref(h)))
+    self._lib, self._h = lib, h
+    nb = ctypes.c_size_t()
+    _lib.check(lib.pjzfdtd_batch_workspace_bytes(h, ctypes.byref(nb)))
+    self.workspace_bytes = nb.value
+    self._ws = None
+    self._stream = None
+    self._keep = None
+
+  def __del__(self):
+    h = getattr(self, "_h", None)
+    if h is not None and h.value:
+      self._lib.pjzfdtd_batch_destroy(h)
+      self._h = None
+
+  def run(self, inputs, graph: bool = True):
+    if len(inputs) != len(self.plans):
+      raise ValueError("one input dict per plan")
+    bufs, keep, outs = [], [], []
+    for plan, kw in zip(self.plans, inputs):
+      b, k, out, out_h = plan.buffers(**kw)
+      bufs.append(b)
+      keep.append(k)
+      outs.append((out, out_h))
+    dev = keep[0][0].device
+    if self._ws is None or self._ws.device != dev:
+      self._ws = torch.empty(max(self.workspace_bytes, 256), dtype=torch.uint8,
+                             device=dev)
+    arr = (_lib.Buffers * len(bufs))(*bufs)
+    cur = torch.cuda.current_stream(dev)
+    if self._stream is None:
+      self._stream = torch.cuda.Stream(device=dev)
+    side = self._stream
+    side.wait_stream(cur)
+    with torch.cuda.device(dev), torch.cuda.stream(side):
+      rc = self._lib.pjzfdtd_batch_run(
+          self._h, arr, ctypes.c_void_p(self._ws.data_ptr()), self._ws.numel(),
+          int(bool(graph)), ctypes.c_void_p(side.cuda_stream))
+    _lib.check(rc)
+    cur.wait_stream(side)
+    for k in keep:
+      for t in k:
+        if t is not None:
+          t.record_stream(side)
+    self._keep = keep  # the captured graph refers to these buffers
+    return outs
+
+  def check_status(self):
+    """Raises TimeoutError if a bounded device wait of any plan gave up."""
+    for i, p in enumerate(self.plans):
+      off = 0
+      # Each plan's workspace sits at its 256-byte aligned offset.
+      for q in self.plans[:i]:
+        off = (off + q.workspace_bytes + 255) // 256 * 256
+      with torch.cuda.device(self._ws.device):
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _lib.check(self._lib.pjzfdtd_plan_status(
+            p._h, ctypes.c_void_p(self._ws.data_ptr() + off), p.workspace_bytes,
+            stream))
