@@ -42,7 +42,9 @@ def _args():
   ap.add_argument("--steps", type=int, default=3)
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="native", choices=["native", "reference"])
-  ap.add_argument("--workload", default="c1", choices=["c0", "c1"])
+  ap.add_argument("--workload", default="c1", choices=["c0", "c1", "c3", "c4"])
+  ap.add_argument("--batch-n", type=int, default=64, help="c3: problems")
+  ap.add_argument("--tune", action="store_true", help="c3: autotune per shape")
   ap.add_argument("--tt", type=int, default=0, help="override time steps")
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--no-e2e", action="store_true")
@@ -323,9 +325,98 @@ def run_native(args):
     torch.distributed.destroy_process_group()
 
 
+def _timed(fn, steps, warmup):
+  import torch
+  for _ in range(warmup):
+    fn()
+  torch.cuda.synchronize()
+  t0 = time.perf_counter()
+  for _ in range(steps):
+    fn()
+  torch.cuda.synchronize()
+  return (time.perf_counter() - t0) / steps
+
+
+def run_batch_c3(args):
+  """c3: many uneven problems in one graph-captured batched run vs the
+  serial loop of the same plans."""
+  import torch
+  from pjz_gb300 import _field, autotune, engine, workloads
+  dev = torch.device("cuda", 0)
+  wls = workloads.batch_c3(n=args.batch_n, **({"tt": args.tt} if args.tt else {}))
+  plans, inputs = [], []
+  for wl in wls:
+    sp = wl.sim_params
+    if args.tune:
+      ty, st, sx = autotune.knobs(wl.domain, sp.pml_widths)
+      sp = sp._replace(launch_params=sp.launch_params._replace(
+          tile_y=ty, stages=st, seg_x=sx))
+    eps = torch.as_tensor(wl.epsilon, device=dev)
+    kw, om = _field._setup(eps, torch.as_tensor(wl.source, device=dev), wl.omega,
+                           wl.source_pos, sp)
+    plan, prof = _field.phasor_plan(kw, om)
+    plans.append(plan)
+    inputs.append(dict(epsilon=eps, absorption_mask=kw["absorption_mask"],
+                       source=prof, waveform=kw["source_waveform"],
+                       out=torch.empty(plan.out_shape(), device=dev)))
+  cells = sum(wl.cell_updates for wl in wls)
+  batch = engine.Batch(plans)
+  t_batch = _timed(lambda: batch.run(inputs, graph=True), args.steps, args.warmup)
+  batch.check_status()
+  t_serial = _timed(lambda: [p.run(**kw) for p, kw in zip(plans, inputs)],
+                    max(1, args.steps // 2), 1)
+  print(json.dumps({
+      "metric": METRIC, "value": cells / t_batch / 1e9, "unit": UNIT,
+      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": t_batch * 1e3, "higher_is_better": True,
+      "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (seeded blurred random designs)",
+      "config": {"workload": f"c3 {len(wls)} uneven problems, batched + graph",
+                 "cell_updates": cells, "tuned": bool(args.tune),
+                 "shapes": sorted({str(w.domain) for w in wls})},
+      "serial_loop": {"value": cells / t_serial / 1e9, "unit": UNIT,
+                      "ms_per_step": t_serial * 1e3},
+      "speedup_vs_serial_loop": t_serial / t_batch,
+      # per batched run: one step launch per time step of the longest
+      # problem, plus per problem two set-up kernels and one record pass per
+      # sample step.
+      "gpu_launches": args.steps * (max(w.sim_params.tt for w in wls) + sum(
+          p.num_samples + 2 for p in plans))}), flush=True)
+
+
+def run_smatrix_c4(args):
+  """c4: 8 forward + 8 unit-adjoint solves of the 8-port device in one
+  batched graph launch vs the serial loop; grads/s."""
+  import torch
+  from pjz_gb300 import smatrix
+  P = smatrix.build_c4(**({"tt": args.tt} if args.tt else {}))
+  s = smatrix.SMatrixSolver(P)
+  t_batch = _timed(lambda: s.run_batched(graph=True), args.steps, args.warmup)
+  S, L, grad = s.results()
+  t_serial = _timed(s.run_serial, max(1, args.steps // 2), 0)
+  cells = s.cell_updates
+  print(json.dumps({
+      "metric": METRIC, "value": 1.0 / t_batch, "unit": "grads/s",
+      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+      "ms_per_step": t_batch * 1e3, "higher_is_better": True,
+      "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+      "data": "synthetic (seeded blurred random 8-port device)",
+      "config": {"workload": "c4 8-port S-matrix, 8 fwd + 8 adjoint, batched",
+                 "domain": list(P.eps.shape[1:]), "time_steps": P.tt,
+                 "freqs": len(P.omega), "objective": float(L)},
+      "gcell_updates_per_s": cells / t_batch / 1e9,
+      "serial_loop": {"value": 1.0 / t_serial, "unit": "grads/s",
+                      "gcell_updates_per_s": cells / t_serial / 1e9},
+      "speedup_vs_serial_loop": t_serial / t_batch}), flush=True)
+
+
 if __name__ == "__main__":
   a = _args()
   if a.impl == "reference":
     run_reference(a)
+  elif a.workload == "c3":
+    run_batch_c3(a)
+  elif a.workload == "c4":
+    run_smatrix_c4(a)
   else:
     run_native(a)

@@ -116,20 +116,23 @@ def waveguide_c0(tt: int = 2000, domain=(128, 128, 32), absorber: int = 16,
                   ((0, 0, 0), (0, 0, 0)))
 
 
-def design_c1(tt: int = 10000, domain=(512, 512, 64), absorber: int = 16,
-              pml: int = 8, design=(50, 50, 6), ww: int = 5,
-              seed: int = 0) -> Workload:
+def design_problem(domain=(512, 512, 64), tt: int = 10000, wavelengths=None,
+                   seed: int = 0, src_x: int = 20, design=(50, 50, 6),
+                   absorber: int = 16, pml: int = 8, name: str = None) -> Workload:
+  """Waveguide in and out along x through a central blurred random design
+  region (voxels uniform in [2.085, 12.25], Gaussian blur sigma 2 cells,
+  clipped), x-normal Gaussian sheet source at domain x = ``src_x``."""
   X, Y, Z = domain
-  lam = np.linspace(1.50, 1.60, ww) if ww > 1 else np.array([1.55])
+  lam = np.atleast_1d(np.asarray(
+      wavelengths if wavelengths is not None else [1.55], np.float64))
   omega = np.array([omega_of(l) for l in lam])
   zz_eps = Z - 2 * pml
   xx, yy = X - 2 * absorber, Y - 2 * absorber
   yc, zc = yy / 2, zz_eps / 2
-  thick = design[2]
-  eps = _layered_eps((xx, yy, zz_eps), (yc - 5.0, yc + 5.0),
-                     (zc - thick / 2, zc + thick / 2))
-  rng = np.random.default_rng(seed)
   dx, dy, dz = design
+  eps = _layered_eps((xx, yy, zz_eps), (yc - 5.0, yc + 5.0),
+                     (zc - dz / 2, zc + dz / 2))
+  rng = np.random.default_rng(seed)
   vox = rng.uniform(EPS_SIO2, EPS_SI, (dx, dy))
   vox = np.clip(_blur(vox, 2.0), EPS_SIO2, EPS_SI)
   x0, y0 = xx // 2 - dx // 2, yy // 2 - dy // 2
@@ -143,9 +146,36 @@ def design_c1(tt: int = 10000, domain=(512, 512, 64), absorber: int = 16,
                  absorption_padding=absorber, absorption_coeff=ABSORBER_COEFF,
                  pml_widths=(pml, pml), use_reduced_precision=False,
                  launch_params=LaunchParams(zz=Z))
-  return Workload(f"c1 design {X}x{Y}x{Z}", eps.astype(np.float32), src, omega,
-                  20 - absorber, sp, tuple(domain),
+  return Workload(name or f"design {X}x{Y}x{Z}", eps.astype(np.float32), src,
+                  omega, src_x - absorber, sp, tuple(domain),
                   ((x0, y0, z0), (dx, dy, dz)))
+
+
+def design_c1(tt: int = 10000, domain=(512, 512, 64), absorber: int = 16,
+              pml: int = 8, design=(50, 50, 6), ww: int = 5,
+              seed: int = 0) -> Workload:
+  X, Y, Z = domain
+  lam = np.linspace(1.50, 1.60, ww) if ww > 1 else np.array([1.55])
+  return design_problem(domain, tt, lam, seed, 20, design, absorber, pml,
+                        name=f"c1 design {X}x{Y}x{Z}")
+
+
+def batch_c3(n: int = 64, tt: int = 6000, seed: int = 2):
+  """Config c3: ``n`` independent problems, x and y drawn from {256, 384,
+  512}, z from {32, 48, 64}, each with its own blurred random design, its
+  own source plane (domain x in [18, 40)) and 1-3 output frequencies evenly
+  spread over 1.50-1.60 um; ``tt`` steps each."""
+  rng = np.random.default_rng(seed)
+  out = []
+  for k in range(n):
+    X, Y = (int(v) for v in rng.choice([256, 384, 512], 2))
+    Z = int(rng.choice([32, 48, 64]))
+    ww = int(rng.integers(1, 4))
+    lam = np.linspace(1.50, 1.60, ww) if ww > 1 else np.array([1.55])
+    out.append(design_problem((X, Y, Z), tt, lam, seed=1000 + k,
+                              src_x=int(rng.integers(18, 40)),
+                              name=f"c3[{k}] {X}x{Y}x{Z} ww={ww}"))
+  return out
 
 
 def port_profile(wl: Workload, sigma: float = 7.5) -> np.ndarray:
