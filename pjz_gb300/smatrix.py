@@ -9,7 +9,8 @@ j's monitor plane:
 * port i's forward solve records its phasors ``F_i`` on the design box and
   on every port's monitor plane (monitor boxes, no full-field output);
 * port j's *unit adjoint* solve is driven by ``i e^{3iw dt/2} p_j / w~`` on
-  monitor plane j and records ``G_j`` on the design box.  Because the adjoint
+  monitor plane j (divided by the CPML stretch where the window reaches
+  into the z-PML) and records ``G_j`` on the design box.  Because the adjoint
   of forward i is ``sum_j conj(2 m_ij S_ij) x`` (unit adjoint j) by
   linearity, the adjoints do not depend on the forwards, so all 2n solves run
   in one batched, graph-captured launch;
@@ -52,10 +53,12 @@ class SMatrixProblem(NamedTuple):
 def build_c4(domain=(1024, 1024, 64), tt: int = 12000, seed: int = 3,
              device_cells: int = 100, pml: int = 8, absorber: int = 16,
              wavelengths=(1.53, 1.55, 1.57), edge: int = 40,
-             monitor_inset: int = 20, window: int = 30) -> SMatrixProblem:
+             monitor_inset: int = 20, window: int = 30,
+             ramp_steps: int = 500) -> SMatrixProblem:
   """Config c4: 8-port 4x4 um random device (two waveguide ports per side,
   400 nm x 220 nm Si in SiO2), blurred seeded epsilon in [2.085, 12.25],
-  seeded target mask over the port pairs."""
+  seeded target mask over the port pairs.  The sources ramp like pjz's
+  ramped sine over ``ramp_steps`` (full amplitude after ~6 ramps)."""
   X, Y, Z = domain
   rng = np.random.default_rng(seed)
   zc = Z / 2
@@ -92,7 +95,7 @@ def build_c4(domain=(1024, 1024, 64), tt: int = 12000, seed: int = 3,
   n = len(ports)
   target = (rng.uniform(size=(n, n)) < 0.5).astype(np.float64)
   np.fill_diagonal(target, 0.0)
-  ramp = (float(omega.mean() * 0.5 * 500), 4.0)
+  ramp = (float(omega.mean() * 0.5 * ramp_steps), 4.0)
   return SMatrixProblem(eps.astype(np.float32), mask, sig, ports, omega, tt,
                         ((cx - half, cy - half, z0), (device_cells, device_cells,
                                                       z1 - z0)),
@@ -172,13 +175,18 @@ class SMatrixSolver:
       self.inputs.append(dict(source=torch.as_tensor(prof, device=dev),
                               waveform=torch.as_tensor(fwave, dtype=torch.float32,
                                                        device=dev)))
+    # The port windows reach into the z-PML, where the operator is not
+    # reciprocal: the unit adjoint sources are divided by the CPML stretch
+    # (the S^-1 r of the adjoint; the design box lies outside the PML).
+    stretch = _adjoint.cpml_stretch(om, dt, kap, P.pml_sigma, alp, (P.pml, P.pml))
     for port in P.ports:  # unit adjoints
       (mo, ms) = _monitor_box(P, port)
       win = _port_profile(P, port).reshape(ms)
       prof = np.zeros((2 * ww, 3) + ms, np.float32)
       c = _transverse(port)
-      prof[:ww, c] = np.real(coef)[:, None, None, None] * win
-      prof[ww:, c] = np.imag(coef)[:, None, None, None] * win
+      j = coef[:, None, None, None] * win[None] / stretch[:, c, None, None, :]
+      prof[:ww, c] = np.real(j)
+      prof[ww:, c] = np.imag(j)
       plan = engine.Plan(**base, source_origin=mo, source_shape=ms,
                          source_ncols=2 * ww, monitors=[dbox])
       self.plans.append(plan)

@@ -1,19 +1,28 @@
 """Batched S-matrix (n forwards + n unit adjoints in one launch): equal to
-the serial loop of the same solves, and its epsilon-gradient against a
-directional central difference of the objective."""
+the serial loop of the same solves, equal to the same method in FP64 on the
+CPU oracle, whose gradient matches FP64 central differences.
+
+Finite differences of the FP32 forward are not used here: the objective of
+this geometry is ~600 (unnormalised overlaps next to the sources), so its
+FP32 rounding noise (~1e-7 relative) swamps differences at delta-eps 1e-3.
+"""
 
 import numpy as np
 import pytest
 import torch
 
+from oracle import smatrix as osm
 from pjz_gb300 import smatrix
 
 pytestmark = pytest.mark.gpu
 
 
-def _small(tt=6000, **kw):
+def _small(tt=9000, **kw):
+  # Three frequencies 20 nm apart sample over 5928 steps (interval 988), so
+  # the window must start after the (100-step) ramp has settled.
   return smatrix.build_c4(domain=(256, 256, 32), tt=tt, device_cells=40, edge=24,
-                          monitor_inset=12, window=16, pml=4, **kw)
+                          monitor_inset=12, window=16, pml=4, ramp_steps=100,
+                          **kw)
 
 
 def test_batched_equals_serial(native):
@@ -31,25 +40,39 @@ def test_batched_equals_serial(native):
   s.batch.check_status()
 
 
-def test_smatrix_gradient_vs_directional_difference(native):
-  P = _small()
+def _tiny():
+  return smatrix.build_c4(domain=(80, 80, 16), tt=9000, device_cells=16, edge=10,
+                          monitor_inset=6, window=8, pml=3, ramp_steps=100)
+
+
+def test_smatrix_matches_fp64_oracle_and_finite_differences(native):
+  """GPU batched S, objective and gradient against the same method restated
+  in FP64 on the CPU oracle; the FP64 gradient against FP64 central
+  differences (delta-eps 1e-3) at design voxels."""
+  P = _tiny()
   s = smatrix.SMatrixSolver(P)
   s.run_batched()
   S, L, grad = s.results()
-  assert torch.isfinite(S).all() and L.item() > 0
-  (bx, by, bz), (nx, ny, nz) = P.design_box
-  rng = np.random.default_rng(7)
-  v = np.zeros_like(P.eps)
-  v[:, bx:bx + nx, by:by + ny, bz:bz + nz] = rng.choice([-1.0, 1.0], (3, nx, ny, nz))
-
-  def L_of(eps):
-    q = smatrix.SMatrixSolver(P._replace(eps=eps.astype(np.float32)))
-    q.run_batched(graph=False)
-    return q.results()[1].item()
-
-  d = 1e-2
-  fd = (L_of(P.eps + d * v) - L_of(P.eps - d * v)) / (2 * d)
-  ad = float((grad.cpu().numpy() * v[:, bx:bx + nx, by:by + ny, bz:bz + nz]).sum())
-  err = abs(fd - ad) / abs(fd)
-  print(f"S-matrix directional derivative: fd {fd:.6e} adjoint {ad:.6e} rel {err:.2e}")
-  assert err < 2e-3
+  S64, L64, g64 = osm.solve(P)
+  errS = np.linalg.norm(S.cpu().numpy() - S64) / np.linalg.norm(S64)
+  errg = np.linalg.norm(grad.cpu().numpy() - g64) / np.linalg.norm(g64)
+  print(f"S-matrix GPU vs FP64: S {errS:.2e}, L {abs(L.item() - L64) / L64:.2e}, "
+        f"grad {errg:.2e}")
+  assert errS < 1e-4 and errg < 1e-4
+  (bx, by, bz), _ = P.design_box
+  pts = [(1, 5, 7, 2), (0, 9, 3, 3), (1, 12, 12, 1)]
+  fd, ad = [], []
+  for p in pts:
+    d = 1e-3
+    q = (p[0], bx + p[1], by + p[2], bz + p[3])
+    ep, em = P.eps.copy(), P.eps.copy()
+    ep[q] += d
+    em[q] -= d
+    Lp = osm.solve(P, eps=ep, with_gradient=False)[1]
+    Lm = osm.solve(P, eps=em, with_gradient=False)[1]
+    fd.append((Lp - Lm) / (2 * d))
+    ad.append(g64[p])
+  fd, ad = np.array(fd), np.array(ad)
+  err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
+  print("FP64 S-matrix gradient vs FD:", err, fd, ad)
+  assert err < 1e-3
