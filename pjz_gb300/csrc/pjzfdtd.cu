@@ -263,10 +263,23 @@ void layout(pjzfdtd_plan* pl) {
   pl->bytes = o;
 }
 
-cudaError_t set_stream_smem(size_t bytes) {
-  return cudaFuncSetAttribute(yee_stream_kernel,
+using StreamKernel = void (*)(StreamArgs);
+
+// The streamed kernel for a plan: its (zz, tile_y) specialisation when one
+// exists, else the generic instantiation.
+StreamKernel stream_kernel_for(const pjzfdtd_plan* pl) {
+  const int z = pl->p.zz, ty = pl->tile_y;
+#define PJZ_PICK(ZC, TYC) \
+  if (z == ZC && ty == TYC) return yee_stream_kernel<ZC, TYC>;
+  PJZ_STREAM_SHAPES(PJZ_PICK)
+#undef PJZ_PICK
+  return yee_stream_kernel<0, 0>;
+}
+
+cudaError_t set_stream_smem(const pjzfdtd_plan* pl) {
+  return cudaFuncSetAttribute(stream_kernel_for(pl),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)bytes);
+                              (int)pl->smem);
 }
 
 int32_t resolve_seg_x(pjzfdtd_plan* pl) {
@@ -280,9 +293,9 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 1;
   if (pl->kernel == 2) {
-    CUDA_TRY(set_stream_smem(pl->smem));
+    CUDA_TRY(set_stream_smem(pl));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, yee_stream_kernel, pl->threads, pl->smem));
+        &per_sm, stream_kernel_for(pl), pl->threads, pl->smem));
   } else {
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, yee_step_kernel, pl->threads, pl->smem));
@@ -511,11 +524,15 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   if (n0 == 0 && (rc = run_init(pl, b, ws, st, true))) return rc;
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
-  if (pl->kernel == 2) CUDA_TRY(set_stream_smem(pl->smem));
+  StreamKernel sk = nullptr;
+  if (pl->kernel == 2) {
+    CUDA_TRY(set_stream_smem(pl));
+    sk = stream_kernel_for(pl);
+  }
   for (int n = n0; n < n1; ++n) {
     const StepArgs a = step_args(pl, b, ws, n);
     if (pl->kernel == 2)
-      yee_stream_kernel<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
+      sk<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
     else
       yee_step_kernel<<<grid, pl->threads, pl->smem, st>>>(a);
     CUDA_TRY(cudaGetLastError());

@@ -188,11 +188,16 @@ __device__ __forceinline__ void compute_sync(int nthreads) {
 //               results sit in output buffer b = (x - x0) & 1 (count = warps);
 //   free[b]  -- the producer's bulk stores finished reading buffer b.
 // One CTA's work: tile `tile` of y rows and segment `seg` of x planes of the
-// problem described by `sa`.
+// problem described by `sa`.  ZC / TYC fix zz / tile_y at compile time for
+// the common thin-z shapes (every shared-memory offset then folds into an
+// immediate); 0 means "read it from the arguments".
+template <int ZC, int TYC>
 __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
                                             int seg, float* sm) {
   const StepArgs& a = sa.s;
-  const int X = a.X, Y = a.Y, Z = a.Z, TY = a.tile_y;
+  const int X = a.X, Y = a.Y;
+  const int Z = ZC ? ZC : a.Z;
+  const int TY = TYC ? TYC : a.tile_y;
   const int S = sa.stages;
   const StreamGeom g(TY, Z, a.plo + a.phi);
   const int Pp = g.Pp;
@@ -285,10 +290,10 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       ++nfill;
     }
     bool ok = true;
+    int slot = 0;            // ring slot of plane x
+    uint32_t round = 0;      // fills of that slot before plane x's
     for (int x = x0; x < xe && ok; ++x) {
       const int k = x - x0;
-      const int slot = k % S;
-      const uint32_t round = (uint32_t)(k / S);
       const int b = k & 1;
       ok = mbar_wait_or_abort(&done[slot], round & 1, sa.status, &abort_flag);
       if (!ok) break;
@@ -317,6 +322,10 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       }
       bulk_wait_read_all();
       mbar_arrive(&freeb[b]);
+      if (++slot == S) {
+        slot = 0;
+        ++round;
+      }
     }
     // Drain: every issued fill must land before shared memory is released.
     for (int j = max(0, nfill - S); j < nfill; ++j)
@@ -348,12 +357,10 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
   const float mdt = -a.dt;
   const bool active = rt < rpt;
 
+  int slot = 0, slot1 = S > 1 ? 1 : 0;  // ring slots of planes x and x+1
+  uint32_t round = 0, round1 = S > 1 ? 0 : 1;  // their fill rounds
   for (int x = x0; x < xe; ++x) {
     const int k = x - x0;
-    const int slot = k % S;
-    const int slot1 = (k + 1) % S;
-    const uint32_t round = (uint32_t)(k / S);
-    const uint32_t round1 = (uint32_t)((k + 1) / S);
     const int b = k & 1;
     const bool has_x1 = x + 1 < X;
     bool ok = true;
@@ -522,12 +529,34 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
     if ((tid & 31) == 0) mbar_arrive(&done[slot]);
     // H(x-1) (hprev) is rewritten by the next plane's H phase.
     compute_sync(ncomp);
+    slot = slot1;
+    round = round1;
+    if (++slot1 == S) {
+      slot1 = 0;
+      ++round1;
+    }
   }
 }
 
+// (zz, tile_y) pairs with a compile-time specialisation: the tile heights the
+// host picks for these zz with 4 ring stages.
+#define PJZ_STREAM_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(16, 59)
+
+template <int ZC, int TYC>
 __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) float sm[];
-  stream_tile(sa, blockIdx.x, blockIdx.y, sm);
+  stream_tile<ZC, TYC>(sa, blockIdx.x, blockIdx.y, sm);
+}
+
+// Runs the specialisation matching (zz, tile_y), else the generic body.
+__device__ __forceinline__ void stream_tile_any(const StreamArgs& sa, int tile,
+                                                int seg, float* sm) {
+  const int z = sa.s.Z, ty = sa.s.tile_y;
+#define PJZ_DISPATCH(ZC, TYC) \
+  if (z == ZC && ty == TYC) return stream_tile<ZC, TYC>(sa, tile, seg, sm);
+  PJZ_STREAM_SHAPES(PJZ_DISPATCH)
+#undef PJZ_DISPATCH
+  stream_tile<0, 0>(sa, tile, seg, sm);
 }
 
 // Several independent problems advanced by one step in one launch.  Block b
@@ -546,7 +575,7 @@ __global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs b
   const int4 w = ba.work[blockIdx.x];
   StreamArgs sa = ba.args[(ba.step & 1) * ba.nsim + w.x];
   if (sa.s.snc > 0) sa.s.wave += (long long)ba.step * sa.s.snc;
-  stream_tile(sa, w.y, w.z, sm);
+  stream_tile_any(sa, w.y, w.z, sm);
 }
 
 // Absorber conductivity re-laid out as [x][c][Yp] (Yp % 4 == 0, zero tail)
