@@ -88,7 +88,13 @@ typedef struct pjzfdtd_problem {
   int32_t kernel;              /* launch params: 0 auto, 1 register-marching,
                                   2 bulk-copy streamed (needs zz % 4 == 0) */
   int32_t stages;              /* launch params: streamed ring depth, 0 = auto */
-  int32_t reserved[3];
+  int32_t warps;               /* launch params: streamed compute warps per CTA,
+                                  0 = auto (one row per warp and pass) */
+  int32_t wait_limit_kcycles;  /* bound of every device-side wait in thousands
+                                  of SM cycles, 0 = default (~2 s) */
+  int32_t test_stall_bytes;    /* test hook, 0 in use: the streamed producer
+                                  announces this many bytes more than it
+                                  copies, so waits run out (no fault) */
 } pjzfdtd_problem;
 
 typedef struct pjzfdtd_buffers {

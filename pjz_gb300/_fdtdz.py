@@ -27,6 +27,7 @@ class LaunchParams(NamedTuple):
   zz: int = 0
   kernel: int = 0
   stages: int = 0
+  warps: int = 0
 
 
 def launch_knobs(launch_params: Any) -> LaunchParams:
@@ -123,7 +124,7 @@ def fdtdz(
       source_ncols=2, output_steps=steps, out_mode=engine.OUT_SNAPSHOTS,
       tile_y=knobs.tile_y, seg_x=knobs.seg_x,
       steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
-      stages=knobs.stages))
+      stages=knobs.stages, warps=knobs.warps))
   out, _ = plan.run(epsilon=eps, absorption_mask=mask, source=prof,
                     waveform=wave)
   return out

@@ -257,14 +257,14 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
       output_steps=kw["output_steps"], out_mode=out_mode, weights=weights,
       record_h=record_h, tile_y=knobs.tile_y, seg_x=knobs.seg_x,
       steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
-      stages=knobs.stages))
+      stages=knobs.stages, warps=knobs.warps))
   return plan, prof
 
 
 def _launch_dict(launch_params):
   k = launch_knobs(launch_params)
   return dict(tile_y=k.tile_y, seg_x=k.seg_x, steps_per_pass=k.steps_per_pass,
-              kernel=k.kernel, stages=k.stages)
+              kernel=k.kernel, stages=k.stages, warps=k.warps)
 
 
 class _FieldFn(torch.autograd.Function):

@@ -20,15 +20,15 @@ _PROBLEM_INTS2 = (
     "src_x0", "src_y0", "src_z0", "src_nx", "src_ny", "src_nz", "src_ncols",
     "out_start", "out_stop", "out_step", "out_mode", "out_rows", "record_h",
     "grad_x0", "grad_y0", "grad_z0", "grad_nx", "grad_ny", "grad_nz",
-    "tile_y", "seg_x", "steps_per_pass", "kernel", "stages")
+    "tile_y", "seg_x", "steps_per_pass", "kernel", "stages", "warps",
+    "wait_limit_kcycles", "test_stall_bytes")
 
 
 class Problem(ctypes.Structure):
   """Mirror of ``pjzfdtd_problem``."""
   _fields_ = ([(n, ctypes.c_int32) for n in _PROBLEM_INTS]
               + [("dt", ctypes.c_float)]
-              + [(n, ctypes.c_int32) for n in _PROBLEM_INTS2]
-              + [("reserved", ctypes.c_int32 * 3)])
+              + [(n, ctypes.c_int32) for n in _PROBLEM_INTS2])
 
 
 class Buffers(ctypes.Structure):

@@ -140,7 +140,9 @@ int32_t validate(const pjzfdtd_problem& p) {
     if (p.record_h)
       return fail(PJZFDTD_ERR_INVALID, "record_h is not defined for GRADIENT");
   }
-  if (p.tile_y < 0 || p.seg_x < 0 || p.steps_per_pass < 0)
+  if (p.tile_y < 0 || p.seg_x < 0 || p.steps_per_pass < 0 || p.warps < 0 ||
+      p.wait_limit_kcycles < 0 || p.test_stall_bytes < 0 ||
+      p.test_stall_bytes % 16)
     return fail(PJZFDTD_ERR_INVALID, "launch params must be >= 0");
   return PJZFDTD_OK;
 }
@@ -174,7 +176,14 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
                 "memory", ty, Z, S);
   pl->tile_y = ty;
   pl->stages = S;
-  const int ncomp = ((Z / 2) * std::min(rpt, ty + 1) + 31) / 32 * 32;
+  int ncomp = ((Z / 2) * std::min(rpt, ty + 1) + 31) / 32 * 32;
+  if (pl->p.warps > 0) {
+    if (pl->p.warps * 32 < Z / 2 || pl->p.warps > 15)
+      return fail(PJZFDTD_ERR_INVALID,
+                  "warps=%d must cover one z column (%d threads) and be <= 15",
+                  pl->p.warps, Z / 2);
+    ncomp = pl->p.warps * 32;
+  }
   pl->threads = ncomp + 32;
   pl->smem = StreamGeom(ty, Z, P).bytes(S);
   pl->kernel = 2;
@@ -443,6 +452,9 @@ StreamArgs stream_args(const pjzfdtd_plan* pl, void* ws, const StepArgs& a) {
   sa.status = w.status;
   sa.Yp = pl->Yp;
   sa.mask_ws = w.mask_ws;
+  sa.wait_cycles = pl->p.wait_limit_kcycles > 0
+                       ? 1000LL * pl->p.wait_limit_kcycles : kWaitCycles;
+  sa.stall_bytes = (unsigned)pl->p.test_stall_bytes;
   return sa;
 }
 

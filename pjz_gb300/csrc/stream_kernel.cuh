@@ -38,7 +38,7 @@
 
 namespace pjzfdtd {
 
-constexpr long long kWaitCycles = 4000000000LL;  // ~2 s at 2 GHz
+constexpr long long kWaitCycles = 4000000000LL;  // default bound, ~2 s at 2 GHz
 constexpr int kStatusTimeout = 4;
 
 struct StreamArgs {
@@ -47,6 +47,8 @@ struct StreamArgs {
   int Yp;                                 // padded y length of mask_ws rows
   const float* __restrict__ mask_ws;      // [X][3][Yp]
   int* status;                            // device status word (0 = ok)
+  long long wait_cycles;                  // bound of every wait (SM cycles)
+  unsigned stall_bytes;                   // test hook: unfilled expected bytes
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -80,12 +82,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 
 // Bounded wait; returns false (and sets *status) if the phase never flips.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          int* status) {
+                                          int* status, long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicExch(status, kStatusTimeout);
       return false;
     }
@@ -163,13 +165,14 @@ __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
 // did (`*abort` set); returns false in either case.
 __device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity,
                                                    int* status,
-                                                   volatile int* abort) {
+                                                   volatile int* abort,
+                                                   long long limit) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
   for (;;) {
     if (mbar_try_wait(bar, parity)) return true;
     if (*abort) return false;
-    if (clock64() - t0 > kWaitCycles) {
+    if (clock64() - t0 > limit) {
       atomicExch(status, kStatusTimeout);
       *abort = 1;
       return false;
@@ -262,8 +265,8 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       const uint32_t cbb = (uint32_t)(nrows * Z * 4);
       const uint32_t mbb = (uint32_t)((mb - ma) * 4);
       const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
-      const uint32_t total =
-          3 * eb + (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
+      const uint32_t total = sa.stall_bytes + 3 * eb +
+          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
       mbar_expect_tx(&full[slot], total);
       const long long base = (long long)xp * YZ;
       for (int c = 0; c < 3; ++c)
@@ -295,7 +298,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
     for (int x = x0; x < xe && ok; ++x) {
       const int k = x - x0;
       const int b = k & 1;
-      ok = mbar_wait_or_abort(&done[slot], round & 1, sa.status, &abort_flag);
+      ok = mbar_wait_or_abort(&done[slot], round & 1, sa.status, &abort_flag, sa.wait_cycles);
       if (!ok) break;
       if (x >= xs) {
         float* hcur = hn + (size_t)b * 3 * RHZ;
@@ -327,10 +330,10 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
         ++round;
       }
     }
-    // Drain: every issued fill must land before shared memory is released.
+    // Drain: every issued fill must land before shared memory is released
+    // (bounded, and regardless of an abort).
     for (int j = max(0, nfill - S); j < nfill; ++j)
-      mbar_wait_or_abort(&full[j % S], (uint32_t)(j / S) & 1, sa.status,
-                         &abort_flag);
+      mbar_wait(&full[j % S], (uint32_t)(j / S) & 1, sa.status, sa.wait_cycles);
     bulk_wait_all();
     return;
   }
@@ -364,12 +367,12 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
     const int b = k & 1;
     const bool has_x1 = x + 1 < X;
     bool ok = true;
-    if (k == 0) ok = mbar_wait_or_abort(&full[slot], round & 1, sa.status, &abort_flag);
+    if (k == 0) ok = mbar_wait_or_abort(&full[slot], round & 1, sa.status, &abort_flag, sa.wait_cycles);
     if (ok && has_x1)
-      ok = mbar_wait_or_abort(&full[slot1], round1 & 1, sa.status, &abort_flag);
+      ok = mbar_wait_or_abort(&full[slot1], round1 & 1, sa.status, &abort_flag, sa.wait_cycles);
     if (ok && k >= 2)
       ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
-                              &abort_flag);
+                              &abort_flag, sa.wait_cycles);
 
     const float* st = sm + (size_t)slot * g.stage;
     const float* Es = st + g.e_off;
@@ -386,6 +389,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
 
     // H^{n+1/2}(x) for tile rows 0..TY (y = y0-1 .. y0+TY-1).
     if (ok && active) {
+#pragma unroll 2
       for (int r = rt; r < g.RH; r += rpt) {
         const int y = y0 - 1 + r;
         if (y < 0 || y >= Y) continue;
@@ -448,6 +452,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
     // E^{n+1}(x) for rows 0..TY-1 (y = y0 .. y0+TY-1).
     const bool src_plane = x >= a.sx0 && x < a.sx0 + a.snx;
     if (wr && active) {
+#pragma unroll 2
       for (int r = rt; r < TY; r += rpt) {
         const int y = y0 + r;
         if (y >= Y) continue;

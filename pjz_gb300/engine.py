@@ -59,7 +59,8 @@ class Plan:
                grad_origin: Tuple[int, int, int] = (0, 0, 0),
                grad_shape: Tuple[int, int, int] = (0, 0, 0),
                tile_y: int = 0, seg_x: int = 0, steps_per_pass: int = 0,
-               kernel: int = 0, stages: int = 0, monitors=None):
+               kernel: int = 0, stages: int = 0, monitors=None, warps: int = 0,
+               wait_limit_kcycles: int = 0, test_stall_bytes: int = 0):
     lib = _lib.load()
     p = _lib.Problem()
     p.xx, p.yy, p.zz = (int(v) for v in domain)
@@ -77,7 +78,9 @@ class Plan:
     p.grad_x0, p.grad_y0, p.grad_z0 = (int(v) for v in grad_origin)
     p.grad_nx, p.grad_ny, p.grad_nz = (int(v) for v in grad_shape)
     p.tile_y, p.seg_x, p.steps_per_pass = int(tile_y), int(seg_x), int(steps_per_pass)
-    p.kernel, p.stages = int(kernel), int(stages)
+    p.kernel, p.stages, p.warps = int(kernel), int(stages), int(warps)
+    p.wait_limit_kcycles = int(wait_limit_kcycles)
+    p.test_stall_bytes = int(test_stall_bytes)
     zz = p.zz
     kap, sig, alp = (_f32_host(a) for a in (pml_kappa, pml_sigma, pml_alpha))
     for name, a in (("pml_kappa", kap), ("pml_sigma", sig), ("pml_alpha", alp)):

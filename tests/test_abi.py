@@ -44,7 +44,7 @@ def test_abi_version(lib):
 
 
 def test_struct_sizes_match_header():
-  # 12 ints + float + 22 ints + 5 reserved = 40 x 4 bytes.
+  # 12 ints + float + 27 ints = 40 x 4 bytes.
   assert ctypes.sizeof(_lib.Problem) == 160
   assert ctypes.sizeof(_lib.Buffers) == 8 * 8
 
