@@ -2,12 +2,14 @@
 
 Public API (mirrors pjz's ``src/pjz/_field.py``):
   * :class:`SimParams`, :func:`field` -- time-harmonic fields;
+  * :func:`scatter` -- scattering values between port modes;
   * :func:`fdtdz` -- drop-in for the ``fdtdz_jax.fdtdz`` engine call;
   * :class:`engine.Plan` -- the plan/run API over the C ABI.
 """
 
 from ._field import SimParams, field
 from ._fdtdz import LaunchParams, fdtdz
+from ._scatter import scatter
 from . import engine
 
-__all__ = ["SimParams", "field", "fdtdz", "LaunchParams", "engine"]
+__all__ = ["SimParams", "field", "scatter", "fdtdz", "LaunchParams", "engine"]
