@@ -1,0 +1,114 @@
+"""``fdtdz_jax``-compatible entry points for pjz's JAX code.
+
+pjz imports ``fdtdz_jax`` and calls ``fdtdz_jax.fdtdz(**kw)``
+(``src/pjz/_field.py:6, 254-269``).  This module offers the same call, plus
+``field`` and ``scatter`` with ``jax.custom_vjp`` whose backward runs the
+engine's fused adjoint, so pjz code can switch with::
+
+    import pjz_gb300.jax_shim as fdtdz_jax
+
+Arrays cross between JAX and torch through DLPack (zero-copy on the same
+GPU) when called eagerly; under ``jax.jit`` the call goes through
+``jax.pure_callback`` (a host round trip of the inputs and outputs).  jax
+is not a dependency: importing this module without jax raises ImportError.
+"""
+
+try:
+  import jax
+  import jax.numpy as jnp
+except ImportError as e:  # pragma: no cover - exercised only without jax
+  raise ImportError("pjz_gb300.jax_shim needs jax") from e
+
+from functools import partial
+
+import numpy as np
+import torch
+import torch.utils.dlpack as tdl
+
+from . import _fdtdz, _field, _scatter
+
+
+def _to_torch(x):
+  if isinstance(x, jax.Array):
+    try:
+      return tdl.from_dlpack(x)
+    except (TypeError, RuntimeError, BufferError):
+      return torch.as_tensor(np.asarray(x))
+  if isinstance(x, np.ndarray):
+    return torch.as_tensor(x)
+  return x
+
+
+def _to_jax(t: torch.Tensor):
+  try:
+    return jax.dlpack.from_dlpack(t.contiguous())
+  except (TypeError, RuntimeError, BufferError):
+    return jnp.asarray(t.detach().cpu().numpy())
+
+
+def _concrete(*xs):
+  return not any(isinstance(x, jax.core.Tracer) for x in xs)
+
+
+def fdtdz(**kw):
+  """``fdtdz_jax.fdtdz`` replacement: E snapshots ``(ns, 3, xx, yy, zz)``."""
+  arrays = {k: v for k, v in kw.items() if isinstance(v, (jax.Array, np.ndarray))}
+  if _concrete(*arrays.values()):
+    t = {k: _to_torch(v) for k, v in kw.items()}
+    if not t["epsilon"].is_cuda:
+      t["epsilon"] = t["epsilon"].cuda()
+    return _to_jax(_fdtdz.fdtdz(**t))
+  ns = len(range(*kw["output_steps"]))
+  shape = (ns,) + tuple(kw["epsilon"].shape)
+  static = {k: v for k, v in kw.items() if k not in arrays}
+
+  def host(**a):
+    out = _fdtdz.fdtdz(**{k: torch.as_tensor(np.asarray(v)) for k, v in a.items()},
+                       **static)
+    return out.cpu().numpy()
+
+  return jax.pure_callback(host, jax.ShapeDtypeStruct(shape, jnp.float32),
+                           **arrays)
+
+
+def _field_torch(eps, source, omega, pos, sp, need_grad):
+  e = _to_torch(eps)
+  e = (e.cuda() if not e.is_cuda else e).to(torch.float32)
+  if need_grad:
+    e = e.detach().requires_grad_(True)
+  out = _field.field(e, _to_torch(source), np.asarray(omega), pos, sp)
+  return e, out
+
+
+@partial(jax.custom_vjp, nondiff_argnums=(3, 4))
+def field(epsilon, source, omega, source_pos, sim_params):
+  """pjz ``field`` on the engine; differentiable w.r.t. ``epsilon``."""
+  _, out = _field_torch(epsilon, source, omega, source_pos, sim_params, False)
+  return _to_jax(out)
+
+
+def _field_fwd(epsilon, source, omega, source_pos, sim_params):
+  e, out = _field_torch(epsilon, source, omega, source_pos, sim_params, True)
+  return _to_jax(out.detach()), (e, out)
+
+
+def _field_bwd(source_pos, sim_params, res, g):
+  e, out = res
+  # JAX hands the cotangent of a complex output as conj(dL/dz*)-style
+  # ``g``; torch's grad_outputs wants dL/d(conj z) * 2, i.e. conj(g).
+  gt = torch.conj(_to_torch(g).to(out.device))
+  (ge,) = torch.autograd.grad(out, e, grad_outputs=gt)
+  return _to_jax(ge), None, None
+
+
+field.defvjp(_field_fwd, _field_bwd)
+
+
+def scatter(epsilon, omega, modes, betas, pos, is_fwd, sim_params):
+  """pjz ``scatter`` on the engine; differentiable w.r.t. ``epsilon`` through
+  :func:`field`'s custom VJP."""
+  tm = [_to_torch(m) for m in modes]
+  e = _to_torch(epsilon)
+  sv = _scatter.scatter(e.cuda() if not e.is_cuda else e, np.asarray(omega), tm,
+                        [np.asarray(b) for b in betas], pos, is_fwd, sim_params)
+  return [[_to_jax(s) for s in row] for row in sv]
