@@ -5,8 +5,9 @@ against central finite differences.
   on the CPU oracle, and FD of the FP64 oracle forward (exact arithmetic)
   at interior, region-boundary (edge-extended) and source-plane voxels;
 * c2: the 512x512x64 c1 geometry, objective sum_w |port . E_y(x_out)|^2,
-  16 seeded design voxels, FD (delta-eps 1e-3) of the GPU FP32 forward.
-Tolerance: 1e-3 relative (vector norm over the checked voxels).
+  FD of the GPU FP32 forward along the gradient's sign pattern (1e-3), along
+  a random direction and at single voxels (1e-2, the FP32 noise floor).
+Small cases: 1e-3 relative (vector norm over the checked voxels).
 """
 
 import numpy as np
@@ -107,12 +108,17 @@ def test_c2_gradient_vs_finite_differences(native):
 
   The random design region rings down slowly: the objective is 0.8% off its
   steady state at 10000 steps and settles (1e-6) by 20000, so the check runs
-  20000 steps -- the adjoint returns the steady-state gradient.  The FP32
-  objective carries ~2e-7 of rounding noise (L ~ 2.2), i.e. ~1e-4 on a
-  central difference at delta-eps 1e-3 of a derivative ~1e-3; hence the
-  per-voxel differences use delta-eps 0.1 (third-order truncation below
-  1e-3 here) and the directional derivative over every design voxel uses
-  delta-eps 1e-2.  The delta-eps 1e-3 values are printed for the record.
+  20000 steps -- the adjoint returns the steady-state gradient.
+
+  The FP32 objective (L ~ 2.2) carries about 2e-7 of rounding noise that
+  changes with every perturbed input, so a central difference at step d has
+  noise ~3e-7 / (2 d).  The checks are sized against that floor:
+    * along v = sign(grad) on the design box the derivative is sum |grad|
+      (~10, so noise below 1e-5 relative at d = 1e-3); d = 1e-3 and 2e-3 must
+      agree with each other (truncation) and with the adjoint to 1e-3;
+    * along a random +-1 direction (derivative ~6e-3, noise ~2e-3 relative at
+      d = 1e-2) and at 8 single voxels (delta-eps 0.1, noise ~4e-3 rel-L2)
+      the tolerance is 1e-2.
   """
   wl = workloads.design_c1(tt=20000)
   eps = torch.tensor(wl.epsilon, device=DEV, requires_grad=True)
@@ -129,31 +135,43 @@ def test_c2_gradient_vs_finite_differences(native):
       return workloads.overlap_objective(out, wl, port,
                                          dtype=torch.complex128).item()
 
+  def fd_along(v, d):
+    return (L(wl.epsilon + d * v) - L(wl.epsilon - d * v)) / (2 * d)
+
   (bx, by, bz), (nx, ny, nz) = wl.design_box
+  box = (slice(None), slice(bx, bx + nx), slice(by, by + ny), slice(bz, bz + nz))
+
+  v = np.zeros_like(wl.epsilon)
+  v[box] = np.sign(grad[box])
+  ad_sign = float(np.sum(grad * v))
+  fd1, fd2 = fd_along(v, 1e-3), fd_along(v, 2e-3)
+  err_sign = abs(fd1 - ad_sign) / abs(ad_sign)
+  print(f"c2 along sign(grad): fd(1e-3) {fd1:.8e} fd(2e-3) {fd2:.8e} "
+        f"adjoint {ad_sign:.8e} rel {err_sign:.2e}")
+
   rng = np.random.default_rng(1)
   v = np.zeros_like(wl.epsilon)
-  v[:, bx:bx + nx, by:by + ny, bz:bz + nz] = rng.choice([-1.0, 1.0], (3, nx, ny, nz))
-  d = 1e-2
-  fd_dir = (L(wl.epsilon + d * v) - L(wl.epsilon - d * v)) / (2 * d)
+  v[box] = rng.choice([-1.0, 1.0], (3, nx, ny, nz))
+  fd_dir = fd_along(v, 1e-2)
   ad_dir = float(np.sum(grad * v))
   err_dir = abs(fd_dir - ad_dir) / abs(fd_dir)
-  print(f"c2 directional: fd {fd_dir:.6e} adjoint {ad_dir:.6e} rel {err_dir:.2e}")
+  print(f"c2 random direction: fd {fd_dir:.6e} adjoint {ad_dir:.6e} rel {err_dir:.2e}")
 
   pts = [(1, bx + int(rng.integers(nx)), by + int(rng.integers(ny)),
-          bz + int(rng.integers(nz))) for _ in range(16)]
-  fd, fd3, ad = [], [], []
+          bz + int(rng.integers(nz))) for _ in range(8)]
+  fd, ad = [], []
   for p in pts:
-    for delta, acc in ((0.1, fd), (1e-3, fd3)):
-      ep, em = wl.epsilon.copy(), wl.epsilon.copy()
-      ep[p] += delta
-      em[p] -= delta
-      acc.append((L(ep) - L(em)) / (2 * delta))
+    ep, em = wl.epsilon.copy(), wl.epsilon.copy()
+    ep[p] += 0.1
+    em[p] -= 0.1
+    fd.append((L(ep) - L(em)) / 0.2)
     ad.append(grad[p])
-  fd, fd3, ad = np.array(fd), np.array(fd3), np.array(ad)
+  fd, ad = np.array(fd), np.array(ad)
   err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
-  err3 = np.linalg.norm(fd3 - ad) / np.linalg.norm(fd3)
-  print(f"c2 16 voxels: rel {err:.2e} at delta 0.1, {err3:.2e} at delta 1e-3")
+  print(f"c2 8 voxels: rel {err:.2e} at delta 0.1")
   print("fd(0.1)", fd)
   print("adjoint", ad)
-  assert err_dir < 1e-3
-  assert err < 5e-3
+  assert abs(fd1 - fd2) / abs(fd1) < 1e-3
+  assert err_sign < 1e-3
+  assert err_dir < 1e-2
+  assert err < 1e-2
