@@ -54,6 +54,8 @@ def _args():
   ap.add_argument("--stages", type=int, default=0)
   ap.add_argument("--tile-y", type=int, default=0)
   ap.add_argument("--seg-x", type=int, default=0)
+  ap.add_argument("--spp", type=int, default=0,
+                  help="time steps per launch: 0 auto, 1, 2 (temporal blocking)")
   return ap.parse_args()
 
 
@@ -66,7 +68,8 @@ def _workload(args):
     wl = workloads.design_c1(**kw)
   lp = wl.sim_params.launch_params._replace(
       kernel=getattr(args, "kernel", 0), stages=getattr(args, "stages", 0),
-      tile_y=getattr(args, "tile_y", 0), seg_x=getattr(args, "seg_x", 0))
+      tile_y=getattr(args, "tile_y", 0), seg_x=getattr(args, "seg_x", 0),
+      steps_per_pass=getattr(args, "spp", 0))
   return wl._replace(sim_params=wl.sim_params._replace(launch_params=lp))
 
 

@@ -19,6 +19,7 @@
 #include "../../include/pjzfdtd.h"
 #include "step_kernel.cuh"
 #include "stream_kernel.cuh"
+#include "stream2_kernel.cuh"
 #include "record_kernel.cuh"
 
 using namespace pjzfdtd;
@@ -60,6 +61,11 @@ struct pjzfdtd_plan {
   int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed
   int stages = 0;   // streamed ring depth
   size_t smem = 0;  // dynamic shared memory per CTA
+  // Two-step kernel (steps_per_pass == 2): CTA size, ring depths (ring A in
+  // the low byte, ring B above) and shared memory; same tile as above.
+  int threads2 = 0, stages2 = 0;
+  size_t smem2 = 0;
+  int cur = 0;      // state buffer (0: A, 1: B) holding the current step
   // Recorded boxes (x0, y0, z0, nx, ny, nz) and their offsets in `out`.
   std::vector<std::array<int32_t, 6>> boxes;
   std::vector<size_t> box_off;
@@ -144,15 +150,33 @@ int32_t validate(const pjzfdtd_problem& p) {
       p.wait_limit_kcycles < 0 || p.test_stall_bytes < 0 ||
       p.test_stall_bytes % 16)
     return fail(PJZFDTD_ERR_INVALID, "launch params must be >= 0");
+  if (p.steps_per_pass > 2)
+    return fail(PJZFDTD_ERR_INVALID, "steps_per_pass must be 0 (auto), 1 or 2");
   return PJZFDTD_OK;
 }
 
 constexpr size_t kSmemBudget = 220 * 1024;  // of the 227 KB per CTA
 constexpr int kStreamThreads = 512;
 
+// Two-step kernel geometry for tile height ty: rows per pass the CTA can
+// hold (one compute thread per z-pair, at most kStream2Threads - 32 compute
+// threads) and the ring depths that fit shared memory (3 each when they
+// fit, else 2), or 0 when nothing fits.
+int stream2_rows_cap(int Z) { return (kStream2Threads - 32) / (Z / 2); }
+int stream2_stages(int ty, int Z, int P, int want) {
+  for (int s = want > 0 ? want : 3; s >= 2; --s) {
+    if (Stream2Geom(ty, Z, P).bytes(s, s) <= kSmemBudget) return s;
+    if (want > 0) break;
+  }
+  return 0;
+}
+
 // Streamed kernel: zz % 4 == 0, one compute thread per z-pair of a row,
 // compute threads = (zz / 2) * rows-per-pass rounded up to whole warps, one
 // extra producer warp, and a tile height whose ring fits shared memory.
+// With steps_per_pass 2 (or auto) the tile height is the two-step kernel's
+// (rows y0-2..y0+TY in one pass, its rings in shared memory) and the
+// single-step kernel, used for steps whose state is sampled, shares it.
 int32_t resolve_stream(pjzfdtd_plan* pl) {
   const int Z = pl->p.zz;
   const int P = pl->p.pml_lo + pl->p.pml_hi;
@@ -161,6 +185,35 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   if (S < 2 || S > 8)
     return fail(PJZFDTD_ERR_INVALID, "stages must be in [2, 8], got %d", S);
   int ty = pl->p.tile_y;
+  int spp = pl->p.steps_per_pass;
+  int s2 = 0;
+  if (spp != 1) {
+    const int cap = stream2_rows_cap(Z);
+    int t2 = ty;
+    if (t2 == 0)
+      for (int t = std::min(cap - 3, 64); t >= 1; --t)
+        if (stream2_stages(t, Z, P, pl->p.stages) > 0) {
+          t2 = std::min(t, pl->p.yy);
+          break;
+        }
+    s2 = t2 > 0 ? stream2_stages(t2, Z, P, pl->p.stages) : 0;
+    bool use = t2 > 0 && s2 > 0 && StreamGeom(t2, Z, P).bytes(S) <= kSmemBudget;
+    // Auto keeps one step per pass: the two-step kernel moves about half
+    // the HBM bytes per cell-update but issues ~1.3x the instructions per
+    // cell-update, and both kernels are issue-bound on GB300 (measured on
+    // 512x512x64: 0.192 ms per step with one step per launch, 0.224 ms
+    // with two), so two steps per pass is chosen only on request.
+    if (spp == 0) use = false;
+    if (use) {
+      ty = t2;
+      spp = 2;
+    } else if (spp == 2) {
+      return fail(PJZFDTD_ERR_INVALID,
+                  "two-step tile (tile_y=%d, zz=%d) exceeds shared memory", t2, Z);
+    } else {
+      spp = 1;
+    }
+  }
   if (ty == 0) {
     int best = 0;
     for (int t = 1; t <= 64; ++t) {
@@ -187,6 +240,18 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   pl->threads = ncomp + 32;
   pl->smem = StreamGeom(ty, Z, P).bytes(S);
   pl->kernel = 2;
+  pl->steps_per_pass = spp;
+  if (spp == 2) {
+    const int rows = std::min(stream2_rows_cap(Z), ty + 3);
+    pl->threads2 = ((Z / 2) * rows + 31) / 32 * 32 + 32;
+    bool special = false;
+#define PJZ_IS2(ZC, TYC) special |= (Z == ZC && ty == TYC);
+    PJZ_STREAM2_SHAPES(PJZ_IS2)
+#undef PJZ_IS2
+    if (special) pl->threads2 = std::min(pl->threads2, stream2_bound(Z, ty));
+    pl->stages2 = s2 | (s2 << 8);
+    pl->smem2 = Stream2Geom(ty, Z, P).bytes(s2, s2);
+  }
   return PJZFDTD_OK;
 }
 
@@ -203,6 +268,9 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax))
     return resolve_stream(pl);
   pl->kernel = 1;
+  if (pl->p.steps_per_pass == 2)
+    return fail(PJZFDTD_ERR_UNSUPPORTED,
+                "two steps per pass need the streamed kernel (zz %% 4 == 0)");
   int ty = pl->p.tile_y;
   const int max_rows = kMaxThreads / Z;
   if (max_rows < 3)
@@ -291,6 +359,22 @@ cudaError_t set_stream_smem(const pjzfdtd_plan* pl) {
                               (int)pl->smem);
 }
 
+// The two-step kernel for a plan, by the same rule.
+StreamKernel stream2_kernel_for(const pjzfdtd_plan* pl) {
+  const int z = pl->p.zz, ty = pl->tile_y;
+#define PJZ_PICK2(ZC, TYC) \
+  if (z == ZC && ty == TYC) return yee_stream2_kernel<ZC, TYC>;
+  PJZ_STREAM2_SHAPES(PJZ_PICK2)
+#undef PJZ_PICK2
+  return yee_stream2_kernel<0, 0>;
+}
+
+cudaError_t set_stream2_smem(const pjzfdtd_plan* pl) {
+  return cudaFuncSetAttribute(stream2_kernel_for(pl),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)pl->smem2);
+}
+
 int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   if (pl->seg_x > 0) return PJZFDTD_OK;
   if (pl->p.seg_x > 0) {
@@ -301,7 +385,11 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 1;
-  if (pl->kernel == 2) {
+  if (pl->kernel == 2 && pl->steps_per_pass == 2) {
+    CUDA_TRY(set_stream2_smem(pl));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, stream2_kernel_for(pl), pl->threads2, pl->smem2));
+  } else if (pl->kernel == 2) {
     CUDA_TRY(set_stream_smem(pl));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, stream_kernel_for(pl), pl->threads, pl->smem));
@@ -405,9 +493,10 @@ int32_t run_init(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   return PJZFDTD_OK;
 }
 
-// Step arguments of step n (ping-pong parity and waveform row).
+// Step arguments of a launch starting at step n with the state in buffer
+// `cur` (0: A, 1: B); the launch writes the other buffer.
 StepArgs step_args(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
-                   int n) {
+                   int n, int cur) {
   const pjzfdtd_problem& p = pl->p;
   RunPtrs w(pl, ws);
   StepArgs a;
@@ -434,11 +523,11 @@ StepArgs step_args(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   a.snz = p.src_ncols > 0 ? p.src_nz : 0;
   a.snc = p.src_ncols;
   a.src = b->source;
-  const bool even = (n % 2) == 0;
-  a.fin = even ? w.fa : w.fb;
-  a.fout = even ? w.fb : w.fa;
-  a.psi_in = even ? w.pa : w.pb;
-  a.psi_out = even ? w.pb : w.pa;
+  const bool in_a = cur == 0;
+  a.fin = in_a ? w.fa : w.fb;
+  a.fout = in_a ? w.fb : w.fa;
+  a.psi_in = in_a ? w.pa : w.pb;
+  a.psi_out = in_a ? w.pb : w.pa;
   a.wave = p.src_ncols > 0 ? b->waveform + (size_t)n * p.src_ncols : nullptr;
   return a;
 }
@@ -449,6 +538,7 @@ StreamArgs stream_args(const pjzfdtd_plan* pl, void* ws, const StepArgs& a) {
   std::memset(&sa, 0, sizeof(sa));
   sa.s = a;
   sa.stages = pl->stages;
+  sa.stages2 = pl->stages2;
   sa.status = w.status;
   sa.Yp = pl->Yp;
   sa.mask_ws = w.mask_ws;
@@ -514,13 +604,27 @@ int32_t record_step(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
 }
 
 int32_t run_finish(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
-                   cudaStream_t st) {
+                   cudaStream_t st, int cur) {
   if (!b->fields) return PJZFDTD_OK;
   RunPtrs w(pl, ws);
-  float* fin = (pl->p.tt % 2 == 0) ? w.fa : w.fb;
+  float* fin = cur == 0 ? w.fa : w.fb;
   CUDA_TRY(cudaMemcpyAsync(b->fields, fin, 6 * pl->N * sizeof(float),
                            cudaMemcpyDeviceToDevice, st));
   return PJZFDTD_OK;
+}
+
+// Launch schedule of steps [n0, n1): two steps per launch where the plan
+// allows it and the state between them is not sampled, one step otherwise.
+// Each entry is (first step, steps).
+std::vector<std::pair<int, int>> schedule(const pjzfdtd_plan* pl, int n0, int n1) {
+  std::vector<std::pair<int, int>> out;
+  for (int n = n0; n < n1;) {
+    const bool pair =
+        pl->steps_per_pass == 2 && n + 1 < n1 && !is_sample(pl->p, n);
+    out.emplace_back(n, pair ? 2 : 1);
+    n += pair ? 2 : 1;
+  }
+  return out;
 }
 
 int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
@@ -533,24 +637,37 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   rc = resolve_seg_x(pl);
   if (rc) return rc;
   const pjzfdtd_problem& p = pl->p;
-  if (n0 == 0 && (rc = run_init(pl, b, ws, st, true))) return rc;
+  if (n0 == 0) {
+    if ((rc = run_init(pl, b, ws, st, true))) return rc;
+    pl->cur = 0;
+  }
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
-  StreamKernel sk = nullptr;
+  StreamKernel sk = nullptr, sk2 = nullptr;
   if (pl->kernel == 2) {
     CUDA_TRY(set_stream_smem(pl));
     sk = stream_kernel_for(pl);
   }
-  for (int n = n0; n < n1; ++n) {
-    const StepArgs a = step_args(pl, b, ws, n);
-    if (pl->kernel == 2)
-      sk<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
-    else
-      yee_step_kernel<<<grid, pl->threads, pl->smem, st>>>(a);
-    CUDA_TRY(cudaGetLastError());
-    if (is_sample(p, n) && (rc = record_step(pl, b, ws, n, a.fout, st))) return rc;
+  if (pl->steps_per_pass == 2) {
+    CUDA_TRY(set_stream2_smem(pl));
+    sk2 = stream2_kernel_for(pl);
   }
-  if (n1 == p.tt) return run_finish(pl, b, ws, st);
+  for (const auto& ln : schedule(pl, n0, n1)) {
+    const StepArgs a = step_args(pl, b, ws, ln.first, pl->cur);
+    if (ln.second == 2) {
+      sk2<<<grid, pl->threads2, pl->smem2, st>>>(stream_args(pl, ws, a));
+    } else if (pl->kernel == 2) {
+      sk<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
+    } else {
+      yee_step_kernel<<<grid, pl->threads, pl->smem, st>>>(a);
+    }
+    CUDA_TRY(cudaGetLastError());
+    pl->cur ^= 1;
+    const int last = ln.first + ln.second - 1;
+    if (is_sample(p, last) && (rc = record_step(pl, b, ws, last, a.fout, st)))
+      return rc;
+  }
+  if (n1 == p.tt) return run_finish(pl, b, ws, st, pl->cur);
   return PJZFDTD_OK;
 }
 
@@ -559,10 +676,16 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
 struct pjzfdtd_batch {
   std::vector<pjzfdtd_plan*> plans;
   std::vector<size_t> off;  // workspace offset of each plan
-  size_t off_args = 0, off_work = 0, bytes = 0;
+  size_t off_args = 0, off_work = 0, off_sched = 0, bytes = 0;
   int max_work = 0;
   int tt_max = 0;
   size_t smem = 0;
+  size_t smem2 = 0;       // two-step kernel's shared memory (0: none)
+  // Per launch: the prefix of the work table that runs and which kernels it
+  // needs (bit 0: one step, bit 1: two steps); per problem the launches of
+  // its own schedule (first step, steps).
+  std::vector<int> active, kinds;
+  std::vector<std::vector<std::pair<int, int>>> sched;
   // Cached CUDA graph of a whole run and the buffers it was captured with.
   cudaGraphExec_t exec = nullptr;
   std::vector<pjzfdtd_buffers> gbufs;
@@ -581,7 +704,7 @@ bool same_buffers(const pjzfdtd_buffers& a, const pjzfdtd_buffers& b) {
 
 // Enqueues one whole batched run on `st` (capturable: no host copies).
 int32_t batch_enqueue(pjzfdtd_batch* bt, const pjzfdtd_buffers* bufs, void* ws,
-                      const std::vector<int>& active, cudaStream_t st) {
+                      cudaStream_t st) {
   const int n = (int)bt->plans.size();
   int32_t rc;
   for (int i = 0; i < n; ++i)
@@ -590,24 +713,33 @@ int32_t batch_enqueue(pjzfdtd_batch* bt, const pjzfdtd_buffers* bufs, void* ws,
   BatchArgs ba;
   ba.args = at<const StreamArgs>(ws, bt->off_args);
   ba.work = at<const int4>(ws, bt->off_work);
+  ba.sched = at<const int2>(ws, bt->off_sched);
   ba.nsim = n;
-  for (int step = 0; step < bt->tt_max; ++step) {
-    ba.step = step;
-    if (active[step] > 0) {
-      yee_stream_batch_kernel<<<active[step], kStreamThreads, bt->smem, st>>>(ba);
+  for (int j = 0; j < (int)bt->active.size(); ++j) {
+    ba.launch = j;
+    if (bt->active[j] > 0 && (bt->kinds[j] & 2)) {
+      yee_stream_batch2_kernel<<<bt->active[j], kStream2Threads, bt->smem2, st>>>(ba);
+      CUDA_TRY(cudaGetLastError());
+    }
+    if (bt->active[j] > 0 && (bt->kinds[j] & 1)) {
+      yee_stream_batch_kernel<<<bt->active[j], kStreamThreads, bt->smem, st>>>(ba);
       CUDA_TRY(cudaGetLastError());
     }
     for (int i = 0; i < n; ++i) {
       const pjzfdtd_plan* pl = bt->plans[i];
-      if (step >= pl->p.tt || !is_sample(pl->p, step)) continue;
+      if (j >= (int)bt->sched[i].size()) continue;
+      const auto& ln = bt->sched[i][j];
+      const int last = ln.first + ln.second - 1;
+      if (!is_sample(pl->p, last)) continue;
       void* wsi = at<char>(ws, bt->off[i]);
       RunPtrs w(pl, wsi);
-      const float* fout = (step % 2 == 0) ? w.fb : w.fa;
-      if ((rc = record_step(pl, &bufs[i], wsi, step, fout, st))) return rc;
+      const float* fout = (j % 2 == 0) ? w.fb : w.fa;
+      if ((rc = record_step(pl, &bufs[i], wsi, last, fout, st))) return rc;
     }
   }
   for (int i = 0; i < n; ++i)
-    if ((rc = run_finish(bt->plans[i], &bufs[i], at<char>(ws, bt->off[i]), st)))
+    if ((rc = run_finish(bt->plans[i], &bufs[i], at<char>(ws, bt->off[i]), st,
+                         (int)(bt->sched[i].size() & 1))))
       return rc;
   return PJZFDTD_OK;
 }
@@ -804,6 +936,7 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
     o = align256(o + pl->bytes);
     bt->tt_max = std::max(bt->tt_max, pl->p.tt);
     bt->smem = std::max(bt->smem, pl->smem);
+    bt->smem2 = std::max(bt->smem2, pl->smem2);
     // Segments are at least 8 planes long (or the whole x extent).
     const int tiles = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
     const int minseg = std::min(pl->p.xx, 8);
@@ -813,6 +946,8 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
   o = align256(o + 2 * (size_t)n * sizeof(StreamArgs));
   bt->off_work = o;
   o = align256(o + (size_t)bt->max_work * sizeof(int4));
+  bt->off_sched = o;  // at most one launch per step
+  o = align256(o + (size_t)bt->tt_max * n * sizeof(int2));
   bt->bytes = o;
   *batch = bt;
   return PJZFDTD_OK;
@@ -855,12 +990,16 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
       return PJZFDTD_OK;
     }
   }
-  // Work table, longest-running problems first so that the active entries of
-  // every step form a prefix; per-problem step arguments for both parities.
+  // Launch schedules; work table with the problems of most launches first,
+  // so that the active entries of every launch form a prefix; per-problem
+  // step arguments for both buffer parities.
+  batch->sched.assign(n, {});
+  for (int i = 0; i < n; ++i)
+    batch->sched[i] = schedule(batch->plans[i], 0, batch->plans[i]->p.tt);
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return batch->plans[a]->p.tt > batch->plans[b]->p.tt;
+    return batch->sched[a].size() > batch->sched[b].size();
   });
   std::vector<int4> work;
   std::vector<int> prefix_end(n);
@@ -874,17 +1013,27 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
   }
   if ((int)work.size() > batch->max_work)
     return fail(PJZFDTD_ERR_INVALID, "work table overflow");
-  std::vector<int> active(batch->tt_max, 0);
-  for (int step = 0; step < batch->tt_max; ++step)
-    for (int r = 0; r < n; ++r)
-      if (batch->plans[order[r]]->p.tt > step) active[step] = prefix_end[r];
+  const int nl = (int)batch->sched[order[0]].size();
+  batch->active.assign(nl, 0);
+  batch->kinds.assign(nl, 0);
+  std::vector<int2> table((size_t)nl * n, make_int2(0, 0));
+  for (int r = 0; r < n; ++r) {
+    const int i = order[r];
+    for (int j = 0; j < (int)batch->sched[i].size(); ++j) {
+      batch->active[j] = prefix_end[r];
+      batch->kinds[j] |= batch->sched[i][j].second;
+      table[(size_t)j * n + i] =
+          make_int2(batch->sched[i][j].first, batch->sched[i][j].second);
+    }
+  }
   std::vector<StreamArgs> args(2 * (size_t)n);
   for (int parity = 0; parity < 2; ++parity)
     for (int i = 0; i < n; ++i) {
       void* wsi = at<char>(workspace, batch->off[i]);
-      StepArgs a = step_args(batch->plans[i], &buffers[i], wsi, parity);
-      a.wave = buffers[i].waveform;  // row 0; the kernel adds step * ncols
-      args[(size_t)parity * n + i] = stream_args(batch->plans[i], wsi, a);
+      const pjzfdtd_plan* pl = batch->plans[i];
+      StepArgs a = step_args(pl, &buffers[i], wsi, 0, parity);
+      a.wave = buffers[i].waveform;  // row 0; the kernel adds the step
+      args[(size_t)parity * n + i] = stream_args(pl, wsi, a);
     }
   // Host copies (not capturable from pageable memory) happen before capture.
   CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, batch->off_args), args.data(),
@@ -892,6 +1041,8 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
                            st));
   CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, batch->off_work), work.data(),
                            work.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+  CUDA_TRY(cudaMemcpyAsync(at<char>(workspace, batch->off_sched), table.data(),
+                           table.size() * sizeof(int2), cudaMemcpyHostToDevice, st));
   for (int i = 0; i < n; ++i) {
     pjzfdtd_plan* pl = batch->plans[i];
     RunPtrs w(pl, at<char>(workspace, batch->off[i]));
@@ -901,7 +1052,11 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
   CUDA_TRY(cudaFuncSetAttribute(yee_stream_batch_kernel,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)batch->smem));
-  if (!use_graph) return batch_enqueue(batch, buffers, workspace, active, st);
+  if (batch->smem2 > 0)
+    CUDA_TRY(cudaFuncSetAttribute(yee_stream_batch2_kernel,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)batch->smem2));
+  if (!use_graph) return batch_enqueue(batch, buffers, workspace, st);
 
   CUDA_TRY(cudaStreamSynchronize(st));  // host copies above read pageable memory
   if (batch->exec) {
@@ -909,7 +1064,7 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
     batch->exec = nullptr;
   }
   CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-  rc = batch_enqueue(batch, buffers, workspace, active, st);
+  rc = batch_enqueue(batch, buffers, workspace, st);
   cudaGraph_t graph = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(st, &graph);
   if (rc) {

@@ -43,7 +43,8 @@ constexpr int kStatusTimeout = 4;
 
 struct StreamArgs {
   StepArgs s;
-  int stages;
+  int stages;                             // single-step ring depth
+  int stages2;                            // two-step rings: A | B << 8
   int Yp;                                 // padded y length of mask_ws rows
   const float* __restrict__ mask_ws;      // [X][3][Yp]
   int* status;                            // device status word (0 = ok)
@@ -564,22 +565,26 @@ __device__ __forceinline__ void stream_tile_any(const StreamArgs& sa, int tile,
   stream_tile<0, 0>(sa, tile, seg, sm);
 }
 
-// Several independent problems advanced by one step in one launch.  Block b
-// runs entry `work[b] = (sim, tile, seg)`; `args[parity][sim]` holds each
-// problem's step arguments for even / odd steps (ping-pong buffers) with the
-// waveform row pointer at step 0, offset here by the step index.
+// Batched launch of one step per problem: block b runs entry work[b] =
+// (sim, tile, seg) when that problem's launch `launch` of its schedule is a
+// single step (sched[launch * nsim + sim] = (first step, steps));
+// args[(launch & 1) * nsim + sim] holds its arguments for the buffer parity
+// of this launch with the waveform row pointer at step 0.
 struct BatchArgs {
   const StreamArgs* __restrict__ args;  // [2][nsim]
   const int4* __restrict__ work;        // [nwork]: sim, tile, seg, unused
+  const int2* __restrict__ sched;       // [launches][nsim]: step, steps
   int nsim;
-  int step;
+  int launch;
 };
 
 __global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs ba) {
   extern __shared__ __align__(16) float sm[];
   const int4 w = ba.work[blockIdx.x];
-  StreamArgs sa = ba.args[(ba.step & 1) * ba.nsim + w.x];
-  if (sa.s.snc > 0) sa.s.wave += (long long)ba.step * sa.s.snc;
+  const int2 sc = ba.sched[(size_t)ba.launch * ba.nsim + w.x];
+  if (sc.y != 1) return;
+  StreamArgs sa = ba.args[(ba.launch & 1) * ba.nsim + w.x];
+  if (sa.s.snc > 0) sa.s.wave += (long long)sc.x * sa.s.snc;
   stream_tile_any(sa, w.y, w.z, sm);
 }
 

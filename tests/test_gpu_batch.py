@@ -62,17 +62,22 @@ def _mixed_cases():
   return [random_problem(40 + i, **s) for i, s in enumerate(specs)]
 
 
+@pytest.mark.parametrize("spp", ["1", "2", "mixed"])
 @pytest.mark.parametrize("graph", [False, True])
-def test_batch_equals_single_runs(native, graph):
+def test_batch_equals_single_runs(native, graph, spp):
+  """Uneven problems in one batch -- one step per launch, two, or a mix --
+  equal their single-plan runs bit for bit (and the oracle)."""
   cases = _mixed_cases()
   plans, refs, ins = [], [], []
   for k, case in enumerate(cases):
     ns = len(range(*case["output_steps"]))
+    knob = dict(steps_per_pass=int(spp) if spp != "mixed" else 1 + k % 2)
     if k % 2:
       w = np.random.default_rng(k).normal(size=(6, ns)).astype(np.float32)
-      p = plan_of(case, engine.OUT_PHASORS, w)
+      p = plan_of(case, engine.OUT_PHASORS, w, **knob)
     else:
-      p = plan_of(case)
+      p = plan_of(case, **knob)
+    assert p.launch_config()["steps_per_pass"] == knob["steps_per_pass"]
     ref, _ = p.run(**inputs_of(case))
     plans.append(p)
     refs.append(ref)

@@ -25,7 +25,8 @@ def dev(a):
 
 
 def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
-            tile_y=0, seg_x=0, fields=None, split=None, kernel=0, stages=0):
+            tile_y=0, seg_x=0, fields=None, split=None, kernel=0, stages=0,
+            steps_per_pass=0):
   p = engine.Plan(domain=case["domain"], offset=case["offset"],
                   region=case["eps"].shape[1:], tt=case["tt"], dt=case["dt"],
                   pml_widths=case["pml_widths"], pml_kappa=case["kappa"],
@@ -35,7 +36,10 @@ def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
                   source_ncols=case["source_profile"].shape[0],
                   output_steps=case["output_steps"], out_mode=out_mode,
                   weights=weights, record_h=record_h, tile_y=tile_y,
-                  seg_x=seg_x, kernel=kernel, stages=stages)
+                  seg_x=seg_x, kernel=kernel, stages=stages,
+                  steps_per_pass=steps_per_pass)
+  if steps_per_pass:
+    assert p.launch_config()["steps_per_pass"] == steps_per_pass
   args = dict(epsilon=dev(case["eps"]), absorption_mask=dev(case["mask"]),
               source=dev(case["source_profile"]), waveform=dev(case["waveform"]))
   f = None if fields is None else dev(fields)
@@ -51,18 +55,22 @@ def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
   return cpu(out), cpu(out_h), cpu(f)
 
 
-KERNELS = [1, 2]  # register-marching, bulk-copy streamed
+# register-marching; bulk-copy streamed one step per launch; streamed two
+# steps per launch (temporal blocking)
+VARIANTS = [dict(kernel=1), dict(kernel=2, steps_per_pass=1),
+            dict(kernel=2, steps_per_pass=2)]
+VIDS = ["reg", "stream1", "stream2"]
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
 @pytest.mark.parametrize("src", ["x", "y", "z"])
 @pytest.mark.parametrize("Z,pml", [(16, (2, 2)), (24, (3, 5)), (48, (8, 8)),
                                    (64, (8, 8)), (12, (0, 0))])
-def test_snapshots_bit_exact(native, src, Z, pml, kernel):
+def test_snapshots_bit_exact(native, src, Z, pml, variant):
   case = random_problem(hash((src, Z)) % 1000, Z=Z, pml=pml, src=src,
                         src_pos=5 if src == "z" else 7)
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, kernel=kernel)
+  got, _, _ = gpu_run(case, **variant)
   assert np.array_equal(got, want), np.abs(got - want).max()
 
 
@@ -73,61 +81,97 @@ def test_odd_z_uses_register_marching_kernel(native):
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
-def test_use_z_as_batch_bit_exact(native, kernel):
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
+def test_use_z_as_batch_bit_exact(native, variant):
   case = random_problem(3, Z=20, batch=True, pml=(0, 0))
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, kernel=kernel)
+  got, _, _ = gpu_run(case, **variant)
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
 @pytest.mark.parametrize("tile_y,seg_x", [(1, 1), (2, 3), (5, 24), (7, 8), (0, 2)])
-def test_launch_geometry_does_not_change_results(native, tile_y, seg_x, kernel):
+def test_launch_geometry_does_not_change_results(native, tile_y, seg_x, variant):
   case = random_problem(4, X=26, Y=23, Z=16)
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, tile_y=tile_y, seg_x=seg_x, kernel=kernel)
+  got, _, _ = gpu_run(case, tile_y=tile_y, seg_x=seg_x, **variant)
   assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("spp", [1, 2])
 @pytest.mark.parametrize("stages", [2, 3, 5, 8])
-def test_stream_ring_depth_does_not_change_results(native, stages):
+def test_stream_ring_depth_does_not_change_results(native, stages, spp):
   case = random_problem(12, X=30, Y=21, Z=32, pml=(4, 4))
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, kernel=2, stages=stages, tile_y=6, seg_x=7)
+  got, _, _ = gpu_run(case, kernel=2, stages=stages, tile_y=6, seg_x=7,
+                      steps_per_pass=spp)
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
-def test_record_h_and_final_state(native, kernel):
+@pytest.mark.parametrize("tt,steps", [(47, (5, 47, 3)), (40, (0, 40, 1)),
+                                      (41, (-6, 41, 2)), (9, (8, 9, 1))])
+def test_two_step_schedule_around_samples(native, tt, steps):
+  """Two steps per launch except where a sampled state sits between them:
+  odd and even sample steps, every step sampled, odd tt, and sample steps
+  before 0.  Results stay bit-identical to the oracle."""
+  case = random_problem(13, X=22, Y=19, Z=16, pml=(2, 3), tt=tt, steps=steps)
+  want = oracle.run(**oracle_kwargs(case), record_h=True)
+  got, got_h, _ = gpu_run(case, kernel=2, steps_per_pass=2, record_h=True,
+                          tile_y=4, seg_x=5)
+  assert np.array_equal(got, want["out"])
+  assert np.array_equal(got_h, want["out_h"])
+
+
+@pytest.mark.parametrize("Z,tile_y", [(64, 14), (64, 11), (64, 10), (48, 15)])
+@pytest.mark.parametrize("pml", [(8, 8), (3, 5), (0, 0)])
+@pytest.mark.parametrize("src", ["x", "z"])
+def test_two_step_specialised_shapes(native, Z, tile_y, pml, src):
+  """The compile-time (zz, tile_y) shapes of the two-step kernel (z-pairs
+  straddling a slab edge when a PML width is odd) are bit-identical to the
+  oracle, with a tile boundary inside the domain."""
+  case = random_problem(15, X=19, Y=2 * tile_y + 5, Z=Z, pml=pml, src=src,
+                        tt=24, steps=(9, 24, 4))
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, kernel=2, steps_per_pass=2, tile_y=tile_y, seg_x=6)
+  assert np.array_equal(got, want)
+
+
+def test_two_step_rejected_for_register_kernel(native):
+  case = random_problem(14, Z=18, pml=(3, 2))
+  with pytest.raises(NotImplementedError, match="two steps"):
+    gpu_run(case, kernel=1, steps_per_pass=2)
+
+
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
+def test_record_h_and_final_state(native, variant):
   case = random_problem(5, Z=24, pml=(4, 4))
   f0 = np.random.default_rng(9).normal(size=(6,) + case["domain"]).astype(np.float32)
   want = oracle.run(**oracle_kwargs(case), record_h=True, fields=f0.copy())
   got, got_h, got_f = gpu_run(case, record_h=True, fields=f0.copy(),
-                              kernel=kernel)
+                              **variant)
   assert np.array_equal(got, want["out"])
   assert np.array_equal(got_h, want["out_h"])
   assert np.array_equal(got_f, want["fields"])
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
-def test_run_steps_chaining_matches_single_run(native, kernel):
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
+def test_run_steps_chaining_matches_single_run(native, variant):
   case = random_problem(6, tt=60, steps=(20, 60, 7))
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, split=33, kernel=kernel)
+  got, _, _ = gpu_run(case, split=33, **variant)
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
 @pytest.mark.parametrize("rows", [2, 10, 32])
-def test_phasor_projection_bit_exact(native, rows, kernel):
+def test_phasor_projection_bit_exact(native, rows, variant):
   case = random_problem(7, Z=32, pml=(4, 4), steps=(10, 48, 3))
   ns = len(range(*case["output_steps"]))
   w = np.random.default_rng(rows).normal(size=(rows, ns)).astype(np.float32)
   want = oracle.run(**oracle_kwargs(case), mode="project", weights=w,
                     record_h=True)
   got, got_h, _ = gpu_run(case, out_mode=engine.OUT_PHASORS, weights=w,
-                          record_h=True, kernel=kernel)
+                          record_h=True, **variant)
   assert np.array_equal(got, want["out"])
   assert np.array_equal(got_h, want["out_h"])
 
@@ -188,8 +232,8 @@ def test_field_c0_full_vs_fp32_and_fp64_oracle(native):
   assert err < 1e-5
 
 
-@pytest.mark.parametrize("kernel", KERNELS)
-def test_c1_size_short_run_bit_exact(native, kernel):
+@pytest.mark.parametrize("variant", VARIANTS, ids=VIDS)
+def test_c1_size_short_run_bit_exact(native, variant):
   """Full 512x512x64 domain for 24 steps against the FP32 oracle."""
   wl = workloads.design_c1(tt=24, ww=5)
   sp = wl.sim_params
@@ -205,7 +249,7 @@ def test_c1_size_short_run_bit_exact(native, kernel):
               source_profile=prof, waveform=kw["source_waveform"],
               output_steps=steps, domain=domain)
   want = oracle.run(**oracle_kwargs(case))["out"]
-  got, _, _ = gpu_run(case, kernel=kernel)
+  got, _, _ = gpu_run(case, **variant)
   assert np.array_equal(got, want)
 
 
