@@ -136,13 +136,14 @@ def _peaks():
 
 
 def _profile_traffic(name):
-  """Per-cell-update DRAM bytes of the step kernel from a committed ncu
+  """DRAM bytes per cell per launch of the step kernel from a committed ncu
   summary (profiles/<name>.json), or None."""
   path = os.path.join(ROOT, "profiles", f"{name}.json")
   try:
     with open(path) as f:
       d = json.load(f)
-    return float(d["dram_bytes_per_cell_update"]), d
+    return float(d.get("dram_bytes_per_cell_per_launch",
+                       d["dram_bytes_per_cell_update"])), d
   except (OSError, KeyError, ValueError):
     return None, None
 
@@ -265,17 +266,25 @@ def run_native(args):
   plan.run(**run_args, out=out, steps=(1, 1 + nl))
   k1.record(stream)
   torch.cuda.synchronize()
-  launch_ms = k0.elapsed_time(k1) / nl
+  # Each launch reads and writes the state once, whether it advances one
+  # step or two (temporal blocking): 60 B per cell per launch.
+  cfg0 = plan.launch_config()
+  launches = plan.step_launches(1, 1 + nl)
+  launch_ms = k0.elapsed_time(k1) / launches
   cells_per_launch = int(np.prod(wl.domain))
   achieved = BYTES_PER_CELL * cells_per_launch / (launch_ms / 1e3) / 1e9
+  effective = BYTES_PER_CELL * cells_per_launch * nl / launches / (launch_ms / 1e3) / 1e9
   peak, peak_kind = _peaks()
-  kname = "yee_stream" if plan.launch_config()["kernel"] == 2 else "yee_step"
+  kname = ("yee_stream2" if cfg0["steps_per_pass"] == 2 else "yee_stream"
+           if cfg0["kernel"] == 2 else "yee_step")
   bpc, prof_d = _profile_traffic(f"{kname}_{args.workload}")
   roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
               "unit": "GB/s", "frac": achieved / peak,
               "peak_source": f"hbm_gbs of {peak_kind}",
               "kernel": f"{kname}_kernel",
               "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells_per_launch,
+              "steps_per_launch": nl / launches,
+              "effective_gbs_per_step": effective,
               "launch_ms": launch_ms,
               "traffic": None if bpc is None else bpc * cells_per_launch}
 
@@ -318,14 +327,36 @@ def run_native(args):
                    "parallelism": "replicas" if world > 1 else "single",
                    "launch": cfg},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        # per solve: tt step launches, the cb and absorber set-up kernels and
-        # one record pass per sample step.
-        "gpu_launches": args.steps * (sp.tt + 2 + plan.num_samples),
+        # per solve: the step launches of its schedule, the cb and absorber
+        # set-up kernels and one record pass per sample step.
+        "gpu_launches": args.steps * (plan.step_launches() + 2 + plan.num_samples),
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
   if world > 1:
     torch.distributed.destroy_process_group()
+
+
+def _alternate(fa, fb, reps, clock_path):
+  """Times ``fa`` and ``fb`` alternately ``reps`` times each (after their
+  warm-up elsewhere) so that clock and power state affect both alike;
+  returns (mean seconds of fa, mean seconds of fb, clock record)."""
+  import torch
+  clocks = Clocks(0, clock_path)
+  ta, tb = [], []
+  for _ in range(reps):
+    for fn, acc in ((fb, tb), (fa, ta)):
+      torch.cuda.synchronize()
+      t0 = time.perf_counter()
+      fn()
+      torch.cuda.synchronize()
+      acc.append(time.perf_counter() - t0)
+  return statistics.mean(ta), statistics.mean(tb), clocks.stop()
+
+
+def _clock_path(tag):
+  d = os.path.join(ROOT, "gpurun_out")
+  return os.path.join(d if os.path.isdir(d) else "/tmp", f"clocks_{tag}.csv")
 
 
 def _timed(fn, steps, warmup):
@@ -351,9 +382,8 @@ def run_batch_c3(args):
   for wl in wls:
     sp = wl.sim_params
     if args.tune:
-      ty, st, sx = autotune.knobs(wl.domain, sp.pml_widths)
       sp = sp._replace(launch_params=sp.launch_params._replace(
-          tile_y=ty, stages=st, seg_x=sx))
+          **autotune.knobs(wl.domain, sp.pml_widths)))
     eps = torch.as_tensor(wl.epsilon, device=dev)
     kw, om = _field._setup(eps, torch.as_tensor(wl.source, device=dev), wl.omega,
                            wl.source_pos, sp)
@@ -364,10 +394,14 @@ def run_batch_c3(args):
                        out=torch.empty(plan.out_shape(), device=dev)))
   cells = sum(wl.cell_updates for wl in wls)
   batch = engine.Batch(plans)
-  t_batch = _timed(lambda: batch.run(inputs, graph=True), args.steps, args.warmup)
+  run_batch = lambda: batch.run(inputs, graph=True)
+  run_serial = lambda: [p.run(**kw) for p, kw in zip(plans, inputs)]
+  for _ in range(args.warmup):  # graph capture, workspaces, clocks up
+    run_batch()
+  run_serial()
+  t_batch, t_serial, clk = _alternate(run_batch, run_serial, args.steps,
+                                      _clock_path("c3"))
   batch.check_status()
-  t_serial = _timed(lambda: [p.run(**kw) for p, kw in zip(plans, inputs)],
-                    max(1, args.steps // 2), 1)
   print(json.dumps({
       "metric": METRIC, "value": cells / t_batch / 1e9, "unit": UNIT,
       "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
@@ -380,10 +414,12 @@ def run_batch_c3(args):
       "serial_loop": {"value": cells / t_serial / 1e9, "unit": UNIT,
                       "ms_per_step": t_serial * 1e3},
       "speedup_vs_serial_loop": t_serial / t_batch,
-      # per batched run: one step launch per time step of the longest
-      # problem, plus per problem two set-up kernels and one record pass per
-      # sample step.
-      "gpu_launches": args.steps * (max(w.sim_params.tt for w in wls) + sum(
+      "timing": "batched and serial runs alternated after warm-up",
+      "clocks": clk,
+      # per batched run: one step launch per launch of the longest schedule
+      # (a launch that mixes one- and two-step problems runs two kernels),
+      # plus per problem two set-up kernels and one record pass per sample.
+      "gpu_launches": args.steps * (max(p.step_launches() for p in plans) + sum(
           p.num_samples + 2 for p in plans))}), flush=True)
 
 
@@ -394,9 +430,16 @@ def run_smatrix_c4(args):
   from pjz_gb300 import smatrix
   P = smatrix.build_c4(**({"tt": args.tt} if args.tt else {}))
   s = smatrix.SMatrixSolver(P)
-  t_batch = _timed(lambda: s.run_batched(graph=True), args.steps, args.warmup)
+  dev = torch.device("cuda", 0)
+  s.run_batched(graph=True)  # graph capture and batch workspace
+  for p in s.plans:  # the serial loop's workspaces, outside the timing
+    p.workspace(dev)
+  # One repetition of each arm per 3 requested steps: a repetition of either
+  # arm is 16 solves of 12000 steps on 1024x1024x64 (over two minutes).
+  t_batch, t_serial, clk = _alternate(lambda: s.run_batched(graph=True),
+                                      s.run_serial, max(1, args.steps // 3),
+                                      _clock_path("c4"))
   S, L, grad = s.results()
-  t_serial = _timed(s.run_serial, max(1, args.steps // 2), 0)
   cells = s.cell_updates
   print(json.dumps({
       "metric": METRIC, "value": 1.0 / t_batch, "unit": "grads/s",
@@ -410,7 +453,9 @@ def run_smatrix_c4(args):
       "gcell_updates_per_s": cells / t_batch / 1e9,
       "serial_loop": {"value": 1.0 / t_serial, "unit": "grads/s",
                       "gcell_updates_per_s": cells / t_serial / 1e9},
-      "speedup_vs_serial_loop": t_serial / t_batch}), flush=True)
+      "speedup_vs_serial_loop": t_serial / t_batch,
+      "timing": "batched and serial runs alternated after warm-up",
+      "clocks": clk}), flush=True)
 
 
 if __name__ == "__main__":

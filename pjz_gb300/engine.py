@@ -177,6 +177,22 @@ class Plan:
     return dict(zip(("tile_y", "seg_x", "threads", "steps_per_pass", "kernel",
                      "stages"), (v.value for v in vals)))
 
+  def step_launches(self, n0: int = 0, n1: int = None) -> int:
+    """Step-kernel launches for steps [n0, n1): the engine runs two steps
+    per launch when the plan has two steps per pass and the state between
+    them is not sampled, one step otherwise (the schedule of the C
+    library's run loop)."""
+    p = self.problem
+    n1 = p.tt if n1 is None else n1
+    two = self.launch_config()["steps_per_pass"] == 2
+    sampled = lambda n: (p.out_mode != OUT_NONE and p.out_start <= n < p.out_stop
+                         and (n - p.out_start) % p.out_step == 0)
+    count, n = 0, n0
+    while n < n1:
+      n += 2 if (two and n + 1 < n1 and not sampled(n)) else 1
+      count += 1
+    return count
+
   def check_status(self, device=None):
     """Raises TimeoutError if a bounded device-side wait of the work queued
     so far gave up (synchronises torch's current stream)."""
