@@ -29,7 +29,8 @@ def test_tuned_knobs_are_valid_and_exact(native, tmp_path, monkeypatch):
                   source_origin=case["source_origin"],
                   source_shape=case["source_profile"].shape[2:],
                   source_ncols=case["source_profile"].shape[0],
-                  output_steps=case["output_steps"], kernel=2, **k)
+                  output_steps=case["output_steps"], out_mode=engine.OUT_SNAPSHOTS,
+                  kernel=2, **k)
   t = lambda a: torch.as_tensor(np.ascontiguousarray(a), device=DEV)
   out, _ = p.run(epsilon=t(case["eps"]), absorption_mask=t(case["mask"]),
                  source=t(case["source_profile"]), waveform=t(case["waveform"]))
