@@ -17,10 +17,14 @@
 #include <vector>
 
 #include "../../include/pjzfdtd.h"
+// This translation unit defines the small set-up kernels and the
+// register-marching step kernel; the streamed kernels live in kern_*.cu.
+#define PJZ_HOST_KERNELS
 #include "step_kernel.cuh"
 #include "stream_kernel.cuh"
 #include "stream2_kernel.cuh"
 #include "record_kernel.cuh"
+#include "kernel_table.cuh"
 
 using namespace pjzfdtd;
 
@@ -66,6 +70,9 @@ struct pjzfdtd_plan {
   int threads2 = 0, stages2 = 0;
   size_t smem2 = 0;
   int cur = 0;      // state buffer (0: A, 1: B) holding the current step
+  // Ring-carried source rows (single-step kernel): floats per ring slot
+  // (0: the source is read from global memory) and rows per block.
+  int src_ring = 0, src_rows = 0;
   // Recorded boxes (x0, y0, z0, nx, ny, nz) and their offsets in `out`.
   std::vector<std::array<int32_t, 6>> boxes;
   std::vector<size_t> box_off;
@@ -156,6 +163,10 @@ int32_t validate(const pjzfdtd_problem& p) {
 }
 
 constexpr size_t kSmemBudget = 220 * 1024;  // of the 227 KB per CTA
+// Dynamic shared memory a CTA may request: 227 KB less a margin for the
+// kernels' static shared memory (abort flag, waveform row cache; the batch
+// kernel holds one per inlined tile shape, 1.3 KB).
+constexpr size_t kSmemMax = 227 * 1024 - 2048;
 constexpr int kStreamThreads = 512;
 
 // Two-step kernel geometry for tile height ty: rows per pass the CTA can
@@ -240,6 +251,22 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   pl->threads = ncomp + 32;
   pl->smem = StreamGeom(ty, Z, P).bytes(S);
   pl->kernel = 2;
+  // Carry the source box rows in the ring (one bulk copy per column and
+  // component per plane, `stages` planes ahead like the fields) when each
+  // row is whole 16-byte units and the slots still fit; a box of many rows
+  // (a plane crossing the whole tile) keeps the global loads -- it is
+  // crossed by few planes.
+  pl->src_ring = pl->src_rows = 0;
+  const pjzfdtd_problem& q = pl->p;
+  if (q.src_ncols > 0 && q.src_nz % 4 == 0) {
+    const int rows = std::min(ty, q.src_ny);
+    const int sw = q.src_ncols * 3 * rows * q.src_nz;
+    if (rows > 0 && StreamGeom(ty, Z, P, sw).bytes(S) <= kSmemMax) {
+      pl->src_ring = sw;
+      pl->src_rows = rows;
+      pl->smem = StreamGeom(ty, Z, P, sw).bytes(S);
+    }
+  }
   pl->steps_per_pass = spp;
   if (spp == 2) {
     const int rows = std::min(stream2_rows_cap(Z), ty + 3);
@@ -340,33 +367,22 @@ void layout(pjzfdtd_plan* pl) {
   pl->bytes = o;
 }
 
-using StreamKernel = void (*)(StreamArgs);
-
 // The streamed kernel for a plan: its (zz, tile_y) specialisation when one
-// exists, else the generic instantiation.
-StreamKernel stream_kernel_for(const pjzfdtd_plan* pl) {
-  const int z = pl->p.zz, ty = pl->tile_y;
-#define PJZ_PICK(ZC, TYC) \
-  if (z == ZC && ty == TYC) return yee_stream_kernel<ZC, TYC>;
-  PJZ_STREAM_SHAPES(PJZ_PICK)
-#undef PJZ_PICK
-  return yee_stream_kernel<0, 0>;
+// exists, else the generic instantiation; `sr` selects the instantiation
+// whose ring carries the source rows.
+StreamKernel stream_kernel_for(const pjzfdtd_plan* pl, bool sr) {
+  return stream_kernel_ptr(pl->p.zz, pl->tile_y, sr);
 }
 
-cudaError_t set_stream_smem(const pjzfdtd_plan* pl) {
-  return cudaFuncSetAttribute(stream_kernel_for(pl),
+cudaError_t set_stream_smem(const pjzfdtd_plan* pl, bool sr) {
+  return cudaFuncSetAttribute(stream_kernel_for(pl, sr),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)pl->smem);
 }
 
 // The two-step kernel for a plan, by the same rule.
 StreamKernel stream2_kernel_for(const pjzfdtd_plan* pl) {
-  const int z = pl->p.zz, ty = pl->tile_y;
-#define PJZ_PICK2(ZC, TYC) \
-  if (z == ZC && ty == TYC) return yee_stream2_kernel<ZC, TYC>;
-  PJZ_STREAM2_SHAPES(PJZ_PICK2)
-#undef PJZ_PICK2
-  return yee_stream2_kernel<0, 0>;
+  return stream2_kernel_ptr(pl->p.zz, pl->tile_y);
 }
 
 cudaError_t set_stream2_smem(const pjzfdtd_plan* pl) {
@@ -390,9 +406,9 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, stream2_kernel_for(pl), pl->threads2, pl->smem2));
   } else if (pl->kernel == 2) {
-    CUDA_TRY(set_stream_smem(pl));
+    CUDA_TRY(set_stream_smem(pl, pl->src_ring > 0));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, stream_kernel_for(pl), pl->threads, pl->smem));
+        &per_sm, stream_kernel_for(pl, pl->src_ring > 0), pl->threads, pl->smem));
   } else {
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, yee_step_kernel, pl->threads, pl->smem));
@@ -545,6 +561,11 @@ StreamArgs stream_args(const pjzfdtd_plan* pl, void* ws, const StepArgs& a) {
   sa.wait_cycles = pl->p.wait_limit_kcycles > 0
                        ? 1000LL * pl->p.wait_limit_kcycles : kWaitCycles;
   sa.stall_bytes = (unsigned)pl->p.test_stall_bytes;
+  sa.src_ring = pl->src_ring;
+  sa.src_rows = pl->src_rows;
+  // The bulk copies need a 16-byte aligned source profile.
+  sa.src_tma = pl->src_ring > 0 && a.src &&
+               reinterpret_cast<uintptr_t>(a.src) % 16 == 0;
   return sa;
 }
 
@@ -645,8 +666,10 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
   StreamKernel sk = nullptr, sk2 = nullptr;
   if (pl->kernel == 2) {
-    CUDA_TRY(set_stream_smem(pl));
-    sk = stream_kernel_for(pl);
+    // Ring-carried source rows need an aligned source profile (fixed per run).
+    const bool sr = stream_args(pl, ws, step_args(pl, b, ws, n0, pl->cur)).src_tma;
+    CUDA_TRY(set_stream_smem(pl, sr));
+    sk = stream_kernel_for(pl, sr);
   }
   if (pl->steps_per_pass == 2) {
     CUDA_TRY(set_stream2_smem(pl));
@@ -718,11 +741,11 @@ int32_t batch_enqueue(pjzfdtd_batch* bt, const pjzfdtd_buffers* bufs, void* ws,
   for (int j = 0; j < (int)bt->active.size(); ++j) {
     ba.launch = j;
     if (bt->active[j] > 0 && (bt->kinds[j] & 2)) {
-      yee_stream_batch2_kernel<<<bt->active[j], kStream2Threads, bt->smem2, st>>>(ba);
+      batch_kernel_ptr(2)<<<bt->active[j], kStream2Threads, bt->smem2, st>>>(ba);
       CUDA_TRY(cudaGetLastError());
     }
     if (bt->active[j] > 0 && (bt->kinds[j] & 1)) {
-      yee_stream_batch_kernel<<<bt->active[j], kStreamThreads, bt->smem, st>>>(ba);
+      batch_kernel_ptr(1)<<<bt->active[j], kStreamThreads, bt->smem, st>>>(ba);
       CUDA_TRY(cudaGetLastError());
     }
     for (int i = 0; i < n; ++i) {
@@ -1049,11 +1072,11 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
     CUDA_TRY(cudaMemcpyAsync(w.zc, pl->zc.data(), pl->zc.size() * sizeof(float),
                              cudaMemcpyHostToDevice, st));
   }
-  CUDA_TRY(cudaFuncSetAttribute(yee_stream_batch_kernel,
+  CUDA_TRY(cudaFuncSetAttribute(batch_kernel_ptr(1),
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)batch->smem));
   if (batch->smem2 > 0)
-    CUDA_TRY(cudaFuncSetAttribute(yee_stream_batch2_kernel,
+    CUDA_TRY(cudaFuncSetAttribute(batch_kernel_ptr(2),
                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)batch->smem2));
   if (!use_graph) return batch_enqueue(batch, buffers, workspace, st);

@@ -67,6 +67,7 @@ __device__ __forceinline__ void kahan(float* s, float* c, float w, float e) {
   *s = t;
 }
 
+#ifdef PJZ_HOST_KERNELS  // defined in the host translation unit only
 __global__ void __launch_bounds__(kMaxThreads)
     yee_step_kernel(const StepArgs a) {
   extern __shared__ float smem[];
@@ -262,5 +263,7 @@ __global__ void precompute_cb_kernel(const float* __restrict__ eps,
     cb[t] = __fdiv_rn(dt, __fmaf_rn(s, hdt, e));
   }
 }
+
+#endif  // PJZ_HOST_KERNELS
 
 }  // namespace pjzfdtd

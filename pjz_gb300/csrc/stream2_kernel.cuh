@@ -616,13 +616,11 @@ __global__ void __launch_bounds__(stream2_bound(ZC, TYC), 1)
   stream2_tile<ZC, TYC>(sa, blockIdx.x, blockIdx.y, sm);
 }
 
+// Batched two-step tiles: the zz = 64 / tile_y 14 specialisation, else the
+// generic body (each inlined shape costs compile time).
 __device__ __forceinline__ void stream2_tile_any(const StreamArgs& sa, int tile,
                                                  int seg, float* sm) {
-  const int z = sa.s.Z, ty = sa.s.tile_y;
-#define PJZ_DISPATCH2(ZC, TYC) \
-  if (z == ZC && ty == TYC) return stream2_tile<ZC, TYC>(sa, tile, seg, sm);
-  PJZ_STREAM2_SHAPES(PJZ_DISPATCH2)
-#undef PJZ_DISPATCH2
+  if (sa.s.Z == 64 && sa.s.tile_y == 14) return stream2_tile<64, 14>(sa, tile, seg, sm);
   stream2_tile<0, 0>(sa, tile, seg, sm);
 }
 
@@ -632,6 +630,7 @@ __device__ __forceinline__ void stream2_tile_any(const StreamArgs& sa, int tile,
 // nsim + sim] holds its arguments for the buffer parity of this launch with
 // the waveform row pointer at step 0.  A launch whose problems mix one- and
 // two-step entries runs both kernels over the same work prefix.
+#ifdef PJZ_BATCH2_KERNEL  // defined in kern_batch2.cu only
 __global__ void __launch_bounds__(kStream2Threads, 1)
     yee_stream_batch2_kernel(const BatchArgs ba) {
   extern __shared__ __align__(16) float sm[];
@@ -642,5 +641,7 @@ __global__ void __launch_bounds__(kStream2Threads, 1)
   if (sa.s.snc > 0) sa.s.wave += (long long)sc.x * sa.s.snc;
   stream2_tile_any(sa, w.y, w.z, sm);
 }
+
+#endif  // PJZ_BATCH2_KERNEL
 
 }  // namespace pjzfdtd

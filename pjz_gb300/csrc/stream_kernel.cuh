@@ -39,6 +39,7 @@
 namespace pjzfdtd {
 
 constexpr long long kWaitCycles = 4000000000LL;  // default bound, ~2 s at 2 GHz
+constexpr int kWaveCache = 64;  // waveform columns kept in shared memory
 constexpr int kStatusTimeout = 4;
 
 struct StreamArgs {
@@ -50,6 +51,12 @@ struct StreamArgs {
   int* status;                            // device status word (0 = ok)
   long long wait_cycles;                  // bound of every wait (SM cycles)
   unsigned stall_bytes;                   // test hook: unfilled expected bytes
+  // Source rows carried in the ring: floats per slot reserved for them (0:
+  // none), rows per (column, component) block, and whether the producer
+  // fills them (else the E update reads the source from global memory).
+  int src_ring;
+  int src_rows;
+  int src_tma;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -126,11 +133,12 @@ __device__ __forceinline__ void fence_async_smem() {
 
 __host__ __device__ inline int round4(int v) { return (v + 3) & ~3; }
 
-// Shared-memory geometry of one CTA (floats unless noted).
+// Shared-memory geometry of one CTA (floats unless noted); `sw` floats per
+// slot hold the source rows of the plane when the ring carries them.
 struct StreamGeom {
   int TY, Z, P, Pp, RE, RH, MT;
-  int e_off, h_off, c_off, m_off, p_off, stage;  // within a ring slot
-  __host__ __device__ StreamGeom(int ty, int z, int p) {
+  int e_off, h_off, c_off, m_off, p_off, s_off, stage;  // within a ring slot
+  __host__ __device__ StreamGeom(int ty, int z, int p, int sw = 0) {
     TY = ty;
     Z = z;
     P = p;
@@ -143,7 +151,8 @@ struct StreamGeom {
     c_off = h_off + 3 * RH * z;
     m_off = c_off + 3 * ty * z;
     p_off = m_off + 3 * MT;
-    stage = p_off + 4 * RH * Pp;
+    s_off = p_off + 4 * RH * Pp;
+    stage = s_off + sw;
   }
   // CTA buffers after the ring: new H [2][3][RH*Z], new E [2][3][TY*Z],
   // new PML state [2][4][TY*Pp].
@@ -194,8 +203,10 @@ __device__ __forceinline__ void compute_sync(int nthreads) {
 // One CTA's work: tile `tile` of y rows and segment `seg` of x planes of the
 // problem described by `sa`.  ZC / TYC fix zz / tile_y at compile time for
 // the common thin-z shapes (every shared-memory offset then folds into an
-// immediate); 0 means "read it from the arguments".
-template <int ZC, int TYC>
+// immediate); 0 means "read it from the arguments".  SR: the ring carries
+// the source box rows (sa.src_tma); without it the source code path is the
+// plain global-load one and adds nothing to a source-free cell.
+template <int ZC, int TYC, bool SR>
 __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
                                             int seg, float* sm) {
   const StepArgs& a = sa.s;
@@ -203,7 +214,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
   const int Z = ZC ? ZC : a.Z;
   const int TY = TYC ? TYC : a.tile_y;
   const int S = sa.stages;
-  const StreamGeom g(TY, Z, a.plo + a.phi);
+  const StreamGeom g(TY, Z, a.plo + a.phi, sa.src_ring);
   const int Pp = g.Pp;
   float* hn = sm + (size_t)S * g.stage;   // [2][3][RH*Z]
   float* en = hn + g.hn_floats();         // [2][3][TY*Z]
@@ -212,6 +223,10 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
   uint64_t* done = full + S;
   uint64_t* freeb = done + S;
   __shared__ int abort_flag;
+  // This launch's waveform row, read once (ring-carried sources): the E
+  // updates of source cells take it from here instead of global memory.
+  __shared__ float wave_sm[SR ? kWaveCache : 1];
+  const bool wcache = SR && a.snc > 0 && a.snc <= kWaveCache;
 
   const int tid = threadIdx.x;
   const int ncomp = blockDim.x - 32;      // compute threads (multiple of 32)
@@ -237,7 +252,13 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
   const int mb = min(round4(y0 + TY), sa.Yp);
   const int moff = y0 - ma;
   const int RHZ = g.RH * Z, REZ = g.RE * Z;
+  // Source box rows of this tile (ring-carried source blocks).
+  const int srow0 = max(y0, a.sy0);
+  const int nsrow = min(min(y0 + TY, Y), a.sy0 + a.sny) - srow0;
+  const long long sbox = (long long)a.snx * a.sny * a.snz;
+  const int sblk = sa.src_rows * a.snz;  // floats per (column, component)
 
+  if (wcache && tid < a.snc) wave_sm[tid] = a.wave[tid];
   if (tid == 0) {
     abort_flag = 0;
     for (int s = 0; s < S; ++s) {
@@ -266,9 +287,19 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       const uint32_t cbb = (uint32_t)(nrows * Z * 4);
       const uint32_t mbb = (uint32_t)((mb - ma) * 4);
       const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
+      const bool srcp = SR && fullp && nsrow > 0 && xp >= a.sx0 &&
+                        xp < a.sx0 + a.snx;
+      const uint32_t sbb = srcp ? (uint32_t)(nsrow * a.snz * 4) : 0u;
       const uint32_t total = sa.stall_bytes + 3 * eb +
-          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
+          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0) +
+          (uint32_t)a.snc * 3 * sbb;
       mbar_expect_tx(&full[slot], total);
+      if (srcp) {
+        const long long so =
+            ((long long)(xp - a.sx0) * a.sny + (srow0 - a.sy0)) * a.snz;
+        for (int wc = 0; wc < 3 * a.snc; ++wc)
+          bulk_g2s(st + g.s_off + wc * sblk, a.src + wc * sbox + so, sbb, &full[slot]);
+      }
       const long long base = (long long)xp * YZ;
       for (int c = 0; c < 3; ++c)
         bulk_g2s(st + g.e_off + c * REZ + erow0 * Z,
@@ -505,15 +536,28 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
           float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
           if (src_plane && y >= a.sy0 && y < a.sy0 + a.sny && z >= a.sz0 &&
               z < a.sz0 + a.snz) {
-            const long long sb = (long long)a.snx * a.sny * a.snz;
-            const long long si =
-                ((long long)(x - a.sx0) * a.sny + (y - a.sy0)) * a.snz + (z - a.sz0);
+            // Source values from the ring slot of this plane when carried
+            // there, else from global memory; same values, same order.
+            if constexpr (SR) {
+              const float* sv = st + g.s_off + (y - srow0) * a.snz + (z - a.sz0);
+              const float* wv = wcache ? wave_sm : a.wave;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              float j = 0.f;
-              for (int w = 0; w < a.snc; ++w)
-                j = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], j);
-              cur[c] = fsub(cur[c], j);
+              for (int c = 0; c < 3; ++c) {
+                float j = 0.f;
+                for (int w = 0; w < a.snc; ++w) j = ffma(sv[(w * 3 + c) * sblk], wv[w], j);
+                cur[c] = fsub(cur[c], j);
+              }
+            } else {
+              const long long sb = (long long)a.snx * a.sny * a.snz;
+              const long long si =
+                  ((long long)(x - a.sx0) * a.sny + (y - a.sy0)) * a.snz + (z - a.sz0);
+#pragma unroll
+              for (int c = 0; c < 3; ++c) {
+                float j = 0.f;
+                for (int w = 0; w < a.snc; ++w)
+                  j = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], j);
+                cur[c] = fsub(cur[c], j);
+              }
             }
           }
 #pragma unroll
@@ -548,21 +592,27 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
 // host picks for these zz with 4 ring stages.
 #define PJZ_STREAM_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(16, 59)
 
-template <int ZC, int TYC>
+template <int ZC, int TYC, bool SR>
 __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) float sm[];
-  stream_tile<ZC, TYC>(sa, blockIdx.x, blockIdx.y, sm);
+  stream_tile<ZC, TYC, SR>(sa, blockIdx.x, blockIdx.y, sm);
 }
 
-// Runs the specialisation matching (zz, tile_y), else the generic body.
+// Runs the specialisation matching (zz, tile_y, ring-carried source), else
+// the generic body.  Batches keep every plain shape but only the zz = 64
+// shape with ring-carried sources (each inlined shape costs compile time).
 __device__ __forceinline__ void stream_tile_any(const StreamArgs& sa, int tile,
                                                 int seg, float* sm) {
   const int z = sa.s.Z, ty = sa.s.tile_y;
+  if (sa.src_tma) {
+    if (z == 64 && ty == 14) return stream_tile<64, 14, true>(sa, tile, seg, sm);
+    return stream_tile<0, 0, true>(sa, tile, seg, sm);
+  }
 #define PJZ_DISPATCH(ZC, TYC) \
-  if (z == ZC && ty == TYC) return stream_tile<ZC, TYC>(sa, tile, seg, sm);
+  if (z == ZC && ty == TYC) return stream_tile<ZC, TYC, false>(sa, tile, seg, sm);
   PJZ_STREAM_SHAPES(PJZ_DISPATCH)
 #undef PJZ_DISPATCH
-  stream_tile<0, 0>(sa, tile, seg, sm);
+  stream_tile<0, 0, false>(sa, tile, seg, sm);
 }
 
 // Batched launch of one step per problem: block b runs entry work[b] =
@@ -578,6 +628,7 @@ struct BatchArgs {
   int launch;
 };
 
+#ifdef PJZ_BATCH1_KERNEL  // defined in kern_batch.cu only
 __global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs ba) {
   extern __shared__ __align__(16) float sm[];
   const int4 w = ba.work[blockIdx.x];
@@ -588,6 +639,9 @@ __global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs b
   stream_tile_any(sa, w.y, w.z, sm);
 }
 
+#endif  // PJZ_BATCH1_KERNEL
+
+#ifdef PJZ_HOST_KERNELS
 // Absorber conductivity re-laid out as [x][c][Yp] (Yp % 4 == 0, zero tail)
 // so each (x, c) row of a tile is one aligned span.
 __global__ void pad_mask_kernel(const float* __restrict__ mask,
@@ -603,5 +657,7 @@ __global__ void pad_mask_kernel(const float* __restrict__ mask,
     mask_ws[t] = y < Y ? mask[((long long)c * X + x) * Y + y] : 0.f;
   }
 }
+
+#endif  // PJZ_HOST_KERNELS
 
 }  // namespace pjzfdtd
