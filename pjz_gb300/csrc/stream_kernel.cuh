@@ -598,16 +598,13 @@ __global__ void __launch_bounds__(512) yee_stream_kernel(const StreamArgs sa) {
   stream_tile<ZC, TYC, SR>(sa, blockIdx.x, blockIdx.y, sm);
 }
 
-// Runs the specialisation matching (zz, tile_y, ring-carried source), else
-// the generic body.  Batches keep every plain shape but only the zz = 64
-// shape with ring-carried sources (each inlined shape costs compile time).
+// Runs the specialisation matching (zz, tile_y), else the generic body.
+// Batches inline every plain shape; ring-carried sources take the generic
+// body (inlining a specialised one as well made the batch kernel spill).
 __device__ __forceinline__ void stream_tile_any(const StreamArgs& sa, int tile,
                                                 int seg, float* sm) {
   const int z = sa.s.Z, ty = sa.s.tile_y;
-  if (sa.src_tma) {
-    if (z == 64 && ty == 14) return stream_tile<64, 14, true>(sa, tile, seg, sm);
-    return stream_tile<0, 0, true>(sa, tile, seg, sm);
-  }
+  if (sa.src_tma) return stream_tile<0, 0, true>(sa, tile, seg, sm);
 #define PJZ_DISPATCH(ZC, TYC) \
   if (z == ZC && ty == TYC) return stream_tile<ZC, TYC, false>(sa, tile, seg, sm);
   PJZ_STREAM_SHAPES(PJZ_DISPATCH)
