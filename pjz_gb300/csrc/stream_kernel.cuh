@@ -406,7 +406,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
                               &abort_flag, sa.wait_cycles);
 
-    const float* st = sm + (size_t)slot * g.stage;
+    float* st = sm + (size_t)slot * g.stage;  // written only for source J
     const float* Es = st + g.e_off;
     const float* E1 = sm + (size_t)slot1 * g.stage + g.e_off;
     const float* Hs = st + g.h_off;
@@ -478,11 +478,31 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
               make_float2(hnew[c][0], hnew[c][1]);
       }
     }
+    const bool src_plane = x >= a.sx0 && x < a.sx0 + a.snx;
+    if constexpr (SR) {
+      // Source current J_c = sum_w src[w][c] * wave[w] of every source cell
+      // of this tile, shared out over all compute threads (one cell per
+      // thread, columns in order): J_c replaces column 0's value of
+      // component c in the ring slot, read back by the cell's E update
+      // after the barrier below.
+      if (ok && src_plane && nsrow > 0) {
+        const int ncell = nsrow * a.snz;
+        const float* wv = wcache ? wave_sm : a.wave;
+        for (int t = tid; t < ncell; t += ncomp) {
+          float* sv = st + g.s_off + t;  // rows of the box are snz apart
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float j = 0.f;
+            for (int w = 0; w < a.snc; ++w) j = ffma(sv[(w * 3 + c) * sblk], wv[w], j);
+            sv[c * sblk] = j;
+          }
+        }
+      }
+    }
     compute_sync(ncomp);
     if (abort_flag) break;
 
     // E^{n+1}(x) for rows 0..TY-1 (y = y0 .. y0+TY-1).
-    const bool src_plane = x >= a.sx0 && x < a.sx0 + a.snx;
     if (wr && active) {
 #pragma unroll 2
       for (int r = rt; r < TY; r += rpt) {
@@ -539,14 +559,9 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
             // Source values from the ring slot of this plane when carried
             // there, else from global memory; same values, same order.
             if constexpr (SR) {
-              const float* sv = st + g.s_off + (y - srow0) * a.snz + (z - a.sz0);
-              const float* wv = wcache ? wave_sm : a.wave;
+              const float* jv = st + g.s_off + (y - srow0) * a.snz + (z - a.sz0);
 #pragma unroll
-              for (int c = 0; c < 3; ++c) {
-                float j = 0.f;
-                for (int w = 0; w < a.snc; ++w) j = ffma(sv[(w * 3 + c) * sblk], wv[w], j);
-                cur[c] = fsub(cur[c], j);
-              }
+              for (int c = 0; c < 3; ++c) cur[c] = fsub(cur[c], jv[c * sblk]);
             } else {
               const long long sb = (long long)a.snx * a.sny * a.snz;
               const long long si =
