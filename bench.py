@@ -22,6 +22,7 @@ import json
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -243,9 +244,7 @@ def run_native(args):
     plan.run(**run_args, out=out)
   barrier()
   stream = torch.cuda.current_stream(dev)
-  clocks = Clocks(local, os.path.join(ROOT, "gpurun_out", f"clocks_bench_{rank}.csv")
-                  if os.path.isdir(os.path.join(ROOT, "gpurun_out"))
-                  else f"/tmp/clocks_bench_{rank}.csv")
+  clocks = Clocks(local, _clock_path(f"bench_{rank}"))
   e0 = torch.cuda.Event(enable_timing=True)
   e1 = torch.cuda.Event(enable_timing=True)
   e0.record(stream)
@@ -355,8 +354,10 @@ def _alternate(fa, fb, reps, clock_path):
 
 
 def _clock_path(tag):
-  d = os.path.join(ROOT, "gpurun_out")
-  return os.path.join(d if os.path.isdir(d) else "/tmp", f"clocks_{tag}.csv")
+  """Where the nvidia-smi clock samples of a timed region are written
+  (``PJZ_BENCH_CLOCKS_DIR``, default the temp directory)."""
+  d = os.environ.get("PJZ_BENCH_CLOCKS_DIR", tempfile.gettempdir())
+  return os.path.join(d, f"clocks_{tag}.csv")
 
 
 def _timed(fn, steps, warmup):
