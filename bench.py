@@ -291,8 +291,16 @@ def run_native(args):
   if not args.no_e2e:
     eps_h = torch.as_tensor(wl.epsilon).pin_memory()
     src_h = torch.as_tensor(wl.source).pin_memory()
-    res = pjz_gb300.field(eps_h, src_h, wl.omega, wl.source_pos, sp)  # warm
+    # Warm-up: the same W calls as the device loop, so the caching
+    # allocator holds the buffers of a call made while the previous
+    # result is still alive (as in the timed loop).
+    res = pjz_gb300.field(eps_h, src_h, wl.omega, wl.source_pos, sp)
     host = torch.empty(res.shape, dtype=res.dtype).pin_memory()
+    for _ in range(max(1, args.warmup)):
+      res = pjz_gb300.field(eps_h.to(dev, non_blocking=True),
+                            src_h.to(dev, non_blocking=True), wl.omega,
+                            wl.source_pos, sp)
+      host.copy_(res, non_blocking=True)
     barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
