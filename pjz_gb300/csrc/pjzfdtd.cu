@@ -80,7 +80,7 @@ struct pjzfdtd_plan {
   // Workspace layout (byte offsets).
   size_t off_fa = 0, off_fb = 0, off_cb = 0, off_pa = 0, off_pb = 0,
          off_zc = 0, off_comp = 0, off_comph = 0, off_status = 0, off_mask = 0,
-         bytes = 0;
+         off_srcws = 0, bytes = 0;
   int Pp = 0;  // PML state row stride (P rounded up to 4)
   int Yp = 0;  // padded y length of the streamed kernel's absorber copy
 };
@@ -251,14 +251,15 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   pl->threads = ncomp + 32;
   pl->smem = StreamGeom(ty, Z, P).bytes(S);
   pl->kernel = 2;
-  // Carry the source box rows in the ring (one bulk copy per column and
-  // component per plane, `stages` planes ahead like the fields) when each
-  // row is whole 16-byte units and the slots still fit; a box of many rows
-  // (a plane crossing the whole tile) keeps the global loads -- it is
-  // crossed by few planes.
+  // Carry the source box rows in the ring (the box re-laid out as
+  // [x][y][column][component][z] in the workspace, so a tile's rows of one
+  // plane are one bulk copy, `stages` planes ahead like the fields) when a
+  // re-laid row is whole 16-byte units and the slots still fit; a box of
+  // many rows (a plane crossing the whole tile) keeps the global loads --
+  // it is crossed by few planes.
   pl->src_ring = pl->src_rows = 0;
   const pjzfdtd_problem& q = pl->p;
-  if (q.src_ncols > 0 && q.src_nz % 4 == 0) {
+  if (q.src_ncols > 0 && (q.src_ncols * 3 * q.src_nz) % 4 == 0) {
     const int rows = std::min(ty, q.src_ny);
     const int sw = q.src_ncols * 3 * rows * q.src_nz;
     if (rows > 0 && StreamGeom(ty, Z, P, sw).bytes(S) <= kSmemMax) {
@@ -364,6 +365,9 @@ void layout(pjzfdtd_plan* pl) {
   pl->off_comph = take(std::max<size_t>(p.record_h ? comp : 0, 1) * sizeof(float));
   pl->off_status = take(sizeof(int));
   pl->off_mask = take((pl->kernel == 2 ? (size_t)p.xx * 3 * pl->Yp : 1) * sizeof(float));
+  pl->off_srcws = take((pl->src_ring > 0 ? (size_t)p.src_ncols * 3 * p.src_nx *
+                                               p.src_ny * p.src_nz
+                                         : 1) * sizeof(float));
   pl->bytes = o;
 }
 
@@ -451,15 +455,32 @@ int32_t check_buffers(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b,
 
 // Device pointers of one plan's workspace.
 struct RunPtrs {
-  float *fa, *fb, *cb, *pa, *pb, *zc, *comp, *comph, *mask_ws;
+  float *fa, *fb, *cb, *pa, *pb, *zc, *comp, *comph, *mask_ws, *srcws;
   int* status;
   RunPtrs(const pjzfdtd_plan* pl, void* ws)
       : fa(at<float>(ws, pl->off_fa)), fb(at<float>(ws, pl->off_fb)),
         cb(at<float>(ws, pl->off_cb)), pa(at<float>(ws, pl->off_pa)),
         pb(at<float>(ws, pl->off_pb)), zc(at<float>(ws, pl->off_zc)),
         comp(at<float>(ws, pl->off_comp)), comph(at<float>(ws, pl->off_comph)),
-        mask_ws(at<float>(ws, pl->off_mask)), status(at<int>(ws, pl->off_status)) {}
+        mask_ws(at<float>(ws, pl->off_mask)), srcws(at<float>(ws, pl->off_srcws)),
+        status(at<int>(ws, pl->off_status)) {}
 };
+
+// Ring-carried source rows: the source box re-laid out in the workspace
+// (stream-ordered, capturable).  Done by every run call, so a chained call
+// sees the source buffer it is given.
+int32_t relayout_source(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b,
+                        void* ws, cudaStream_t st) {
+  if (pl->src_ring <= 0 || !b->source) return PJZFDTD_OK;
+  const pjzfdtd_problem& p = pl->p;
+  RunPtrs w(pl, ws);
+  const long long n = (long long)p.src_ncols * 3 * p.src_nx * p.src_ny * p.src_nz;
+  source_rows_kernel<<<(int)std::min<long long>((n + 255) / 256, 1 << 16), 256, 0,
+                       st>>>(b->source, w.srcws, p.src_ncols, p.src_nx, p.src_ny,
+                             p.src_nz);
+  CUDA_TRY(cudaGetLastError());
+  return PJZFDTD_OK;
+}
 
 // Start-of-run work (stream-ordered, capturable unless copy_zc): zero the
 // state, outputs and status word, load the initial fields, build the
@@ -506,7 +527,7 @@ int32_t run_init(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
                       st>>>(b->absorption_mask, w.mask_ws, p.xx, p.yy, pl->Yp);
     CUDA_TRY(cudaGetLastError());
   }
-  return PJZFDTD_OK;
+  return relayout_source(pl, b, ws, st);
 }
 
 // Step arguments of a launch starting at step n with the state in buffer
@@ -563,9 +584,8 @@ StreamArgs stream_args(const pjzfdtd_plan* pl, void* ws, const StepArgs& a) {
   sa.stall_bytes = (unsigned)pl->p.test_stall_bytes;
   sa.src_ring = pl->src_ring;
   sa.src_rows = pl->src_rows;
-  // The bulk copies need a 16-byte aligned source profile.
-  sa.src_tma = pl->src_ring > 0 && a.src &&
-               reinterpret_cast<uintptr_t>(a.src) % 16 == 0;
+  sa.src_tma = pl->src_ring > 0 && a.src;
+  sa.src_ws = w.srcws;
   return sa;
 }
 
@@ -661,6 +681,8 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   if (n0 == 0) {
     if ((rc = run_init(pl, b, ws, st, true))) return rc;
     pl->cur = 0;
+  } else if ((rc = relayout_source(pl, b, ws, st))) {
+    return rc;
   }
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);

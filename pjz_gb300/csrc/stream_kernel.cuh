@@ -57,6 +57,9 @@ struct StreamArgs {
   int src_ring;
   int src_rows;
   int src_tma;
+  // The source box re-laid out as [x][y][column][component][z] in the
+  // workspace, so that a tile's box rows of one plane are one span.
+  const float* __restrict__ src_ws;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -255,8 +258,7 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
   // Source box rows of this tile (ring-carried source blocks).
   const int srow0 = max(y0, a.sy0);
   const int nsrow = min(min(y0 + TY, Y), a.sy0 + a.sny) - srow0;
-  const long long sbox = (long long)a.snx * a.sny * a.snz;
-  const int sblk = sa.src_rows * a.snz;  // floats per (column, component)
+  const int srowf = a.snc * 3 * a.snz;  // floats per re-laid source row
 
   if (wcache && tid < a.snc) wave_sm[tid] = a.wave[tid];
   if (tid == 0) {
@@ -289,17 +291,14 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
       const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
       const bool srcp = SR && fullp && nsrow > 0 && xp >= a.sx0 &&
                         xp < a.sx0 + a.snx;
-      const uint32_t sbb = srcp ? (uint32_t)(nsrow * a.snz * 4) : 0u;
+      const uint32_t sbb = srcp ? (uint32_t)(nsrow * srowf * 4) : 0u;
       const uint32_t total = sa.stall_bytes + 3 * eb +
-          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0) +
-          (uint32_t)a.snc * 3 * sbb;
+          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0) + sbb;
       mbar_expect_tx(&full[slot], total);
-      if (srcp) {
-        const long long so =
-            ((long long)(xp - a.sx0) * a.sny + (srow0 - a.sy0)) * a.snz;
-        for (int wc = 0; wc < 3 * a.snc; ++wc)
-          bulk_g2s(st + g.s_off + wc * sblk, a.src + wc * sbox + so, sbb, &full[slot]);
-      }
+      if (srcp)
+        bulk_g2s(st + g.s_off,
+                 sa.src_ws + ((long long)(xp - a.sx0) * a.sny + (srow0 - a.sy0)) * srowf,
+                 sbb, &full[slot]);
       const long long base = (long long)xp * YZ;
       for (int c = 0; c < 3; ++c)
         bulk_g2s(st + g.e_off + c * REZ + erow0 * Z,
@@ -489,12 +488,13 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
         const int ncell = nsrow * a.snz;
         const float* wv = wcache ? wave_sm : a.wave;
         for (int t = tid; t < ncell; t += ncomp) {
-          float* sv = st + g.s_off + t;  // rows of the box are snz apart
+          const int r = t / a.snz;
+          float* sv = st + g.s_off + r * srowf + (t - r * a.snz);
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             float j = 0.f;
-            for (int w = 0; w < a.snc; ++w) j = ffma(sv[(w * 3 + c) * sblk], wv[w], j);
-            sv[c * sblk] = j;
+            for (int w = 0; w < a.snc; ++w) j = ffma(sv[(w * 3 + c) * a.snz], wv[w], j);
+            sv[c * a.snz] = j;
           }
         }
       }
@@ -559,9 +559,9 @@ __device__ __forceinline__ void stream_tile(const StreamArgs& sa, int tile,
             // Source values from the ring slot of this plane when carried
             // there, else from global memory; same values, same order.
             if constexpr (SR) {
-              const float* jv = st + g.s_off + (y - srow0) * a.snz + (z - a.sz0);
+              const float* jv = st + g.s_off + (y - srow0) * srowf + (z - a.sz0);
 #pragma unroll
-              for (int c = 0; c < 3; ++c) cur[c] = fsub(cur[c], jv[c * sblk]);
+              for (int c = 0; c < 3; ++c) cur[c] = fsub(cur[c], jv[c * a.snz]);
             } else {
               const long long sb = (long long)a.snx * a.sny * a.snz;
               const long long si =
@@ -654,6 +654,23 @@ __global__ void __launch_bounds__(512) yee_stream_batch_kernel(const BatchArgs b
 #endif  // PJZ_BATCH1_KERNEL
 
 #ifdef PJZ_HOST_KERNELS
+// Source profile [column][component][x][y][z] (box-local) re-laid out as
+// [x][y][column][component][z], the order the ring carries it in.
+__global__ void source_rows_kernel(const float* __restrict__ src,
+                                   float* __restrict__ dst, int ncols, int nx,
+                                   int ny, int nz) {
+  const int nwc = 3 * ncols;
+  const long long n = (long long)nwc * nx * ny * nz;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int bz = (int)(t % nz);
+    const long long r1 = t / nz;
+    const int wc = (int)(r1 % nwc);
+    const long long xy = r1 / nwc;
+    dst[t] = src[((long long)wc * nx * ny + xy) * nz + bz];
+  }
+}
+
 // Absorber conductivity re-laid out as [x][c][Yp] (Yp % 4 == 0, zero tail)
 // so each (x, c) row of a tile is one aligned span.
 __global__ void pad_mask_kernel(const float* __restrict__ mask,
