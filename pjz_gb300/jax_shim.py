@@ -25,7 +25,7 @@ import numpy as np
 import torch
 import torch.utils.dlpack as tdl
 
-from . import _fdtdz, _field, _scatter
+from . import _fdtdz, _field
 
 
 def _to_torch(x):
@@ -104,11 +104,44 @@ def _field_bwd(source_pos, sim_params, res, g):
 field.defvjp(_field_fwd, _field_bwd)
 
 
+def _slice_jnp(arr, pos, axis):
+  """Transverse components of ``arr`` at ``pos`` along ``axis`` (jnp form of
+  ``_field._transverse_slice``)."""
+  a = "xyz".find(axis)
+  comps = [i for i in range(3) if i != a]
+  arr = arr[..., jnp.asarray(comps), :, :, :]
+  return jax.lax.dynamic_slice_in_dim(arr, pos, 1, axis=arr.ndim - 3 + a)
+
+
+def _overlap_jnp(mode, beta, pos, is_fwd, output):
+  """Two-plane overlap and forward/backward split (jnp form of
+  ``_scatter._overlap`` / ``_amplitudes``)."""
+  beta = jnp.asarray(beta).astype(jnp.complex64)
+  if is_fwd is None:
+    x, at, beta = [0, 0], (pos, pos), beta * 0
+  elif is_fwd:
+    x, at = [1, 2], (pos + 1, pos + 2)
+  else:
+    x, at, beta = [-2, -1], (pos - 2, pos - 1), -beta
+  axis = _field._prop_axis(mode)
+  vals = jnp.stack([jnp.sum(mode * _slice_jnp(output, p, axis),
+                            axis=(-4, -3, -2, -1)) for p in at], axis=-1)
+  bx = beta[:, None] * jnp.asarray(x, jnp.float32)[None, :]
+  a = jnp.stack([jnp.exp(-1j * bx), jnp.exp(1j * bx)], axis=1)
+  return jnp.einsum("...ji,...j->...i", jnp.linalg.pinv(a), vals)
+
+
 def scatter(epsilon, omega, modes, betas, pos, is_fwd, sim_params):
-  """pjz ``scatter`` on the engine; differentiable w.r.t. ``epsilon`` through
-  :func:`field`'s custom VJP."""
-  tm = [_to_torch(m) for m in modes]
-  e = _to_torch(epsilon)
-  sv = _scatter.scatter(e.cuda() if not e.is_cuda else e, np.asarray(omega), tm,
-                        [np.asarray(b) for b in betas], pos, is_fwd, sim_params)
-  return [[_to_jax(s) for s in row] for row in sv]
+  """pjz ``scatter`` (``src/pjz/_field.py:403-442``): one :func:`field` solve
+  per port with the frequency-averaged mode as source, then the two-plane
+  overlap fit; differentiable w.r.t. ``epsilon`` through :func:`field`'s
+  custom VJP (one fused adjoint solve per port)."""
+  modes = [jnp.asarray(m) for m in modes]
+  fields = [field(epsilon, jnp.mean(m, axis=0), omega, p, sim_params)
+            for m, p in zip(modes, pos)]
+  amps = [jnp.ones(jnp.shape(b), jnp.complex64) if fwd is None
+          else _overlap_jnp(m, b, p, fwd, f)[:, 0]
+          for f, m, b, p, fwd in zip(fields, modes, betas, pos, is_fwd)]
+  return [[_overlap_jnp(m, b, p, fwd, f)[:, 1] / a
+           for m, b, p, fwd in zip(modes, betas, pos, is_fwd)]
+          for a, f in zip(amps, fields)]
