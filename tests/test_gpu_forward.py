@@ -136,16 +136,14 @@ def test_two_step_specialised_shapes(native, Z, tile_y, pml, src):
   assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("Z,tile_y,stages", [(64, 14, 4), (64, 18, 3), (48, 19, 4),
-                                            (32, 29, 3)])
+@pytest.mark.parametrize("Z,tile_y,stages", [(64, 14, 4), (48, 19, 4), (32, 29, 3)])
 @pytest.mark.parametrize("pml", [(8, 8), (3, 5)])
 @pytest.mark.parametrize("src", ["x", "y", "z"])
 def test_one_step_specialised_shapes(native, Z, tile_y, stages, pml, src):
-  """The compile-time (zz, tile_y) shapes of the one-step streamed kernel,
-  and zz 64 / tile_y 18 (generic body, H rows in two passes of a 512-thread
-  CTA), with every source orientation (so both the global-load and
-  ring-carried source paths) are bit-identical to the oracle, with a tile
-  boundary inside the domain."""
+  """The compile-time (zz, tile_y) shapes of the one-step streamed kernel
+  with every source orientation (so both the global-load and ring-carried
+  source paths) are bit-identical to the oracle, with a tile boundary
+  inside the domain."""
   case = random_problem(16, X=19, Y=2 * tile_y + 5, Z=Z, pml=pml, src=src,
                         src_pos=5 if src == "z" else 7, tt=24, steps=(9, 24, 4))
   want = oracle.run(**oracle_kwargs(case))["out"]
