@@ -1,7 +1,9 @@
 """The C ABI used from C on the host (no GPU): ``tests/c_abi_host.c`` is
 compiled with gcc against ``include/pjzfdtd.h``, linked with the library and
-run; it creates plans, sizes a workspace, reads the launch geometry and
-checks the error contract of a bad request."""
+run; it creates plans, sizes a workspace, reads the launch geometry, sets
+monitor boxes, creates a batch of plans of different domains and checks the
+error codes of bad requests (including the run-argument checks of a batch,
+which come before any device work)."""
 
 import os
 import shutil
@@ -34,4 +36,5 @@ def test_c_program_uses_the_abi(tmp_path):
   out = subprocess.run([str(exe)], capture_output=True, text=True, env=env)
   print(out.stdout)
   assert out.returncode == 0, out.stdout + out.stderr
-  assert "ok bad region" in out.stdout
+  for line in ("ok monitors", "ok batch", "ok bad region"):
+    assert line in out.stdout
