@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import oracle
-from oracle import pjz_ref, yee_numpy
+from oracle import adjoint, pjz_ref, yee_numpy
 from pjz_gb300 import _field as pf
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_kats.json")
@@ -182,3 +182,94 @@ def test_reciprocity_point_sources():
   np.testing.assert_allclose(ea[:, 2, b[0], b[1], b[2]],
                              eb[:, 0, a[0], a[1], a[2]],
                              rtol=1e-9, atol=1e-12 * np.abs(ea).max())
+
+
+def _cavity_modes(n):
+  """Eigenpairs of the 1-D operator the Yee differences give on n cells:
+  H from forward differences of E with E = 0 beyond the last cell, E from
+  backward differences of H with H = 0 below the first (tridiag(-1, 2, -1)
+  whose first diagonal entry is 1).  Mode m = 1..n: cos(k (i + 1/2)),
+  k = pi (2m - 1) / (2n + 1), eigenvalue 4 sin^2(k / 2)."""
+  i = np.arange(n) + 0.5
+  for m in range(1, n + 1):
+    k = np.pi * (2 * m - 1) / (2 * n + 1)
+    yield np.cos(k * i), 4 * np.sin(k / 2) ** 2
+
+
+def test_yee_dispersion_relation_of_cavity_modes():
+  """With kappa = inf every z-layer is a 2-D Yee problem; the Ez part of
+  each layer's cavity modes evolves, once the source is off, exactly as the
+  leapfrog recurrence of the discrete dispersion relation
+  a(n+1) + a(n-1) = 2 (1 - dt^2 lambda / (2 eps)) a(n), lambda the mode's
+  eigenvalue of the discrete Laplacian."""
+  X, Y, Z, tt, dt, eps_r = 9, 8, 2, 160, 0.5, 2.0
+  wave = np.zeros((tt, 1), np.float32)
+  wave[:3, 0] = (1.0, -1.0, 0.5)
+  prof = np.zeros((1, 3, 1, 1, Z), np.float32)
+  prof[0, 2] = 1.0  # Jz on one (x, y) column
+  zero = np.zeros((Z, 2), np.float32)
+  out = oracle.run(eps=np.full((3, X, Y, Z), eps_r, np.float32), offset=(0, 0, 0),
+                   mask=np.zeros((3, X, Y), np.float32),
+                   kappa=np.full((Z, 2), np.inf, np.float32), sigma=zero, alpha=zero,
+                   dt=dt, tt=tt, pml_widths=(0, 0), source_origin=(3, 2, 0),
+                   source_profile=prof, waveform=wave, precision="f64",
+                   output_steps=(0, tt, 1), mode="snapshot")["out"]
+  ez = out[:, 2, :, :, 0]
+  mx, my = list(_cavity_modes(X)), list(_cavity_modes(Y))
+  checked = 0
+  for m, n in [(0, 0), (1, 2), (4, 1), (8, 7), (6, 3)]:
+    (px, lx), (py, ly) = mx[m], my[n]
+    a = np.einsum("txy,x,y->t", ez, px, py)
+    c = 1 - dt * dt * (lx + ly) / (2 * eps_r)
+    res = a[7:] + a[5:-2] - 2 * c * a[6:-1]
+    assert np.abs(a).max() > 1e-3 * np.abs(ez).max()
+    assert np.abs(res).max() < 1e-11 * np.abs(a).max(), (m, n)
+    # The all-walls-zero sine modes are not this operator's modes.
+    kx, ky = np.pi * (m + 1) / (X + 1), np.pi * (n + 1) / (Y + 1)
+    b = np.einsum("txy,x,y->t", ez, np.sin(kx * np.arange(1, X + 1)),
+                  np.sin(ky * np.arange(1, Y + 1)))
+    cb = 1 - dt * dt * (4 * np.sin(kx / 2) ** 2 + 4 * np.sin(ky / 2) ** 2) / (2 * eps_r)
+    assert np.abs(b[7:] + b[5:-2] - 2 * cb * b[6:-1]).max() > 1e-4 * np.abs(b).max()
+    checked += 1
+  assert checked == 5
+
+
+def test_reciprocity_with_cpml_stretch():
+  """The identity the adjoint rests on, A^T = S A S^-1 with S the CPML
+  z-stretch of each E component: the response Ez(b) to Jx(a) equals
+  S_x(a) / S_z(b) times the response Ex(a) to Jz(b) at every frequency
+  (DTFT of fully decayed responses to a zero-mean pulse), while plain
+  reciprocity fails once a and b sit at unlike depths of the z slabs."""
+  X, Y, Z, tt, dt, pml = 14, 12, 16, 3000, 0.5, (4, 4)
+  rng = np.random.default_rng(6)
+  eps = rng.uniform(1, 3, (3, X, Y, Z)).astype(np.float32)
+  mask = pjz_ref.absorption_mask(X, Y, 4, 0.05).astype(np.float32)
+  sig = pjz_ref.pml_sigma(pml, Z, 0.5, 1.3).astype(np.float32)
+  kappa = np.ones_like(sig)
+  alpha = np.full_like(sig, 0.05)
+  n = np.arange(tt)
+  s = (n - 40) / 8.0
+  wave = (-s * np.exp(-0.5 * s * s)).astype(np.float32)[:, None]
+  a, b = (4, 5, 2), (9, 6, 14)  # both inside the z slabs, unlike depths
+
+  def response(at, comp, probe, pcomp):
+    prof = np.zeros((1, 3, 1, 1, 1), np.float32)
+    prof[0, comp] = 1.0
+    out = oracle.run(eps=eps, offset=(0, 0, 0), mask=mask, kappa=kappa, sigma=sig,
+                     alpha=alpha, dt=dt, tt=tt, pml_widths=pml, source_origin=at,
+                     source_profile=prof, waveform=wave, precision="f64",
+                     output_steps=(0, tt, 1), mode="snapshot")["out"]
+    return out[:, pcomp, probe[0], probe[1], probe[2]]
+
+  zb_from_xa = response(a, 0, b, 2)
+  xa_from_zb = response(b, 2, a, 0)
+  peak = np.abs(zb_from_xa).max()
+  assert np.abs(zb_from_xa[-100:]).max() < 1e-5 * peak  # decayed
+  assert np.abs(zb_from_xa - xa_from_zb).max() > 0.1 * peak
+  for w in (0.3, 0.5, 0.7):
+    ph = np.exp(-1j * w * dt * n)
+    S = adjoint.stretch(np.array([w]), dt, kappa, sig, alpha, pml)[0]
+    ratio = S[0, a[2]] / S[2, b[2]]
+    assert abs(ratio - 1) > 0.2
+    got = (ph @ zb_from_xa) / (ph @ xa_from_zb)
+    assert abs(got - ratio) < 2e-6 * abs(ratio), (w, got, ratio)
