@@ -15,6 +15,9 @@ timed region).  ``roofline`` compares the step kernel's algorithmic bytes
 (60 B per cell-update) per launch against the measured HBM copy bandwidth.
 ``--impl reference`` times the CPU path (the oracle's C Yee transcription
 on all host cores; the reference engine is CUDA-only and not available).
+The native line's ``cpu_baseline`` also carries ``torch_eager``: the same
+update as eager torch ops on CPU tensors (``oracle/yee_torch.py``), all
+host threads, a second CPU figure beside the C port.
 """
 
 import argparse
@@ -149,8 +152,9 @@ def _profile_traffic(name):
     return None, None
 
 
-def cpu_baseline(wl, seconds, threads=0):
-  """Oracle C Yee (FP32, OpenMP) on a bounded number of steps of ``wl``."""
+def cpu_baseline(wl, seconds, threads=0, torch_eager=True):
+  """Oracle C Yee (FP32, OpenMP) on a bounded number of steps of ``wl``;
+  with ``torch_eager`` also the eager-torch CPU port of the same update."""
   import oracle
   from oracle import pjz_ref
   sp = wl.sim_params
@@ -176,11 +180,46 @@ def cpu_baseline(wl, seconds, threads=0):
   n = max(2, min(wl.sim_params.tt, int(seconds / per)))
   dt = run(n)
   cells = np.prod(domain) * n
-  return {"value": cells / dt / 1e9, "unit": UNIT, "cores": threads,
+  out = {"value": cells / dt / 1e9, "unit": UNIT, "cores": threads,
+         "kind": "port",
+         "sample": f"{n} of {wl.sim_params.tt} steps of the {domain[0]}x"
+                   f"{domain[1]}x{domain[2]} domain, oracle/yee.c FP32 + "
+                   f"OpenMP, {dt:.1f} s incl. set-up"}
+  if not torch_eager:
+    return out
+  try:
+    out["torch_eager"] = torch_eager_baseline(kw, org, prof, domain, wl,
+                                              seconds / 2, threads)
+  except Exception as e:  # a second CPU figure only; never fails the line
+    out["torch_eager"] = {"error": f"{type(e).__name__}: {e}"}
+  return out
+
+
+def torch_eager_baseline(kw, org, prof, domain, wl, seconds, threads):
+  """The same update as eager torch ops on CPU tensors (oracle/yee_torch.py,
+  FP32), all host threads; per-step time from runs of 1 and 1 + n steps, so
+  the set-up is excluded."""
+  from oracle import yee_torch
+
+  def run(n):
+    t0 = time.perf_counter()
+    yee_torch.run(eps=kw["epsilon"], offset=kw["offset"], mask=kw["absorption_mask"],
+                  kappa=kw["pml_kappa"], sigma=kw["pml_sigma"], alpha=kw["pml_alpha"],
+                  dt=kw["dt"], tt=n, pml_widths=kw["pml_widths"], source_origin=org,
+                  source_profile=prof, waveform=kw["source_waveform"][:n],
+                  threads=threads)
+    return time.perf_counter() - t0
+
+  t1 = run(1)
+  per = max(run(3) - t1, 1e-6) / 2
+  n = max(2, min(wl.sim_params.tt, int(seconds / per)))
+  dt = run(1 + n) - t1
+  cells = np.prod(domain) * n
+  return {"value": cells / max(dt, 1e-9) / 1e9, "unit": UNIT, "cores": threads,
           "kind": "port",
-          "sample": f"{n} of {wl.sim_params.tt} steps of the {domain[0]}x"
-                    f"{domain[1]}x{domain[2]} domain, oracle/yee.c FP32 + "
-                    f"OpenMP, {dt:.1f} s incl. set-up"}
+          "sample": f"{n} steps of the same domain, oracle/yee_torch.py (eager "
+                    f"torch {__import__('torch').__version__} on CPU tensors, "
+                    f"FP32), set-up excluded"}
 
 
 def run_reference(args):
@@ -190,7 +229,8 @@ def run_reference(args):
   wl = _workload(args)
   vals = []
   for i in range(args.warmup + args.steps):
-    r = cpu_baseline(wl, max(2.0, args.cpu_seconds / max(args.steps, 1)))
+    r = cpu_baseline(wl, max(2.0, args.cpu_seconds / max(args.steps, 1)),
+                     torch_eager=False)
     if i >= args.warmup:
       vals.append(r["value"])
   v = float(np.mean(vals))
