@@ -16,6 +16,11 @@ j's monitor plane:
   in one batched, graph-captured launch;
 * ``dL/d eps = sum_w Re(w~^2 e^{-2iw dt} sum_ij F_i conj(2 m_ij S_ij) G_j)``
   over the design box (the derivation is that of ``_adjoint``).
+
+Across several GPUs (one rank each) the 2n independent solves are shared
+round-robin; each rank runs its share, then one all-gather hands every rank
+the recorded boxes of every solve (the design box and the monitor planes, a
+few MB), and every rank assembles the same S, objective and gradient.
 """
 
 from typing import List, NamedTuple, Tuple
@@ -23,7 +28,7 @@ from typing import List, NamedTuple, Tuple
 import numpy as np
 import torch
 
-from . import _adjoint, _field, engine
+from . import _adjoint, _field, engine, replicas
 from .workloads import (ABSORBER_COEFF, EPS_SI, EPS_SIO2, _blur,
                         _slab_fraction, omega_of)
 
@@ -124,10 +129,14 @@ def _transverse(port: Port):
 
 
 class SMatrixSolver:
-  """The 2n plans (n forwards, n unit adjoints) of one S-matrix problem."""
+  """The 2n plans (n forwards, n unit adjoints) of one S-matrix problem.
+  With ``world`` > 1 this rank runs the solves ``replicas.shard`` gives it
+  (plans 0..n-1 are the forwards, n..2n-1 the unit adjoints)."""
 
-  def __init__(self, P: SMatrixProblem, device=None, launch=None):
+  def __init__(self, P: SMatrixProblem, device=None, launch=None, rank: int = 0,
+               world: int = 1):
     self.P = P
+    self.rank, self.world = rank, world
     dev = torch.device(device or "cuda")
     self.dev = dev
     X, Y, Z = P.eps.shape[1:]
@@ -196,26 +205,42 @@ class SMatrixSolver:
     for kw in self.inputs:
       kw.update(epsilon=self.eps, absorption_mask=self.mask)
     self.outs = [torch.empty(p.out_shape(), device=dev) for p in self.plans]
+    self.mine = replicas.shard(range(len(self.plans)), rank, world)
     self.batch = None
 
   @property
   def cell_updates(self):
+    """Cell-updates of the solves this rank runs."""
     X, Y, Z = self.P.eps.shape[1:]
-    return len(self.plans) * X * Y * Z * self.P.tt
+    return len(self.mine) * X * Y * Z * self.P.tt
 
   def run_batched(self, graph: bool = True):
     if self.batch is None:
-      self.batch = engine.Batch(self.plans)
-    self.batch.run([dict(kw, out=o) for kw, o in zip(self.inputs, self.outs)],
+      self.batch = engine.Batch([self.plans[k] for k in self.mine])
+    self.batch.run([dict(self.inputs[k], out=self.outs[k]) for k in self.mine],
                    graph=graph)
 
   def run_serial(self):
-    """The per-simulation plain loop: the same 2n solves one after another."""
-    for plan, kw, o in zip(self.plans, self.inputs, self.outs):
-      plan.run(**kw, out=o)
+    """The per-simulation plain loop: this rank's solves one after another."""
+    for k in self.mine:
+      self.plans[k].run(**self.inputs[k], out=self.outs[k])
+
+  def exchange(self):
+    """Every rank gets every solve's recorded boxes (an all-gather over the
+    initialised process group; nothing to do on one rank)."""
+    if self.world == 1:
+      return
+    import torch.distributed as dist
+    got = [None] * self.world
+    dist.all_gather_object(got, {k: self.outs[k].cpu() for k in self.mine})
+    for part in got:
+      for k, t in part.items():
+        self.outs[k].copy_(t)
 
   def results(self):
-    """(S (n, n, ww) complex, objective, dL/d-eps (3, design box))."""
+    """(S (n, n, ww) complex, objective, dL/d-eps (3, design box)); with
+    several ranks every rank must call it (it starts with the exchange)."""
+    self.exchange()
     P = self.P
     n, ww = len(P.ports), len(P.omega)
     cplx = lambda a: torch.complex(a[:ww], a[ww:])  # (2ww, 3, ...) -> (ww, ...)
