@@ -46,7 +46,10 @@ def _args():
   ap.add_argument("--steps", type=int, default=3)
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="native", choices=["native", "reference"])
-  ap.add_argument("--workload", default="c1", choices=["c0", "c1", "c3", "c4"])
+  ap.add_argument("--workload", default="c1",
+                  choices=["c0", "c1", "c3", "c4", "src-x", "src-y", "src-y6"],
+                  help="src-*: one-step launches of 512x512x64 with an x-normal, "
+                       "y-normal or 6-column y-normal source box (straggler study)")
   ap.add_argument("--batch-n", type=int, default=64, help="c3: problems")
   ap.add_argument("--tune", action="store_true", help="c3: autotune per shape")
   ap.add_argument("--tt", type=int, default=0, help="override time steps")
@@ -507,9 +510,56 @@ def run_smatrix_c4(args):
       "clocks": clk}), flush=True)
 
 
+SOURCE_BOXES = {  # name: (origin, box shape, waveform columns)
+    "src-x": ((100, 0, 0), (2, 512, 64), 2),
+    "src-y": ((0, 100, 0), (512, 2, 64), 2),
+    "src-y6": ((0, 100, 0), (512, 1, 64), 6),
+}
+
+
+def run_source_box(args):
+  """512x512x64, 8+8 z-PML, one time step per launch, uniform epsilon and a
+  random source in one box orientation: 20 warm-up steps, then 300 steps
+  timed with CUDA events (the run behind the source-orientation profile)."""
+  import torch
+  from pjz_gb300 import engine
+  dev = torch.device("cuda", 0)
+  X, Y, Z = 512, 512, 64
+  tt = max(args.tt, 320) if args.tt else 400
+  org, shp, ncols = SOURCE_BOXES[args.workload]
+  sig = np.zeros((Z, 2), np.float32)
+  sig[:8] = 1.0
+  sig[-8:] = 1.0
+  p = engine.Plan(domain=(X, Y, Z), offset=(0, 0, 0), region=(X, Y, Z), tt=tt,
+                  dt=0.5, pml_widths=(8, 8), pml_kappa=np.ones((Z, 2)),
+                  pml_sigma=sig, pml_alpha=np.zeros((Z, 2)), source_origin=org,
+                  source_shape=shp, source_ncols=ncols, kernel=2)
+  g = torch.Generator(device=dev).manual_seed(0)
+  kw = dict(epsilon=torch.full((3, X, Y, Z), 2.0, device=dev),
+            absorption_mask=torch.zeros((3, X, Y), device=dev),
+            source=torch.randn((ncols, 3) + shp, device=dev, generator=g),
+            waveform=torch.randn((tt, ncols), device=dev, generator=g))
+  p.run(**kw, steps=(0, 20))
+  torch.cuda.synchronize()
+  e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+  e0.record()
+  p.run(**kw, steps=(20, 320))
+  e1.record()
+  torch.cuda.synchronize()
+  p.check_status()
+  ms = e0.elapsed_time(e1) / 300
+  print(json.dumps({
+      "workload": args.workload, "domain": [X, Y, Z], "source_origin": org,
+      "source_box": shp, "source_columns": ncols, "ms_per_step": ms,
+      "value": X * Y * Z / ms / 1e6, "unit": UNIT,
+      "launch": p.launch_config()}), flush=True)
+
+
 if __name__ == "__main__":
   a = _args()
-  if a.impl == "reference":
+  if a.workload in SOURCE_BOXES:
+    run_source_box(a)
+  elif a.impl == "reference":
     run_reference(a)
   elif a.workload == "c3":
     run_batch_c3(a)
