@@ -211,7 +211,8 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
     bool use = t2 > 0 && s2 > 0 && StreamGeom(t2, Z, P).bytes(S) <= kSmemBudget;
     // Auto keeps one step per pass: the two-step kernel moves about half
     // the HBM bytes per cell-update but issues ~1.3x the instructions per
-    // cell-update, and both kernels are issue-bound on GB300 (measured on
+    // cell-update, and on GB300 its time is set on the SM side (instruction
+    // latency with 4-5 warps per scheduler), not by HBM (measured on
     // 512x512x64: 0.192 ms per step with one step per launch, 0.224 ms
     // with two), so two steps per pass is chosen only on request.
     if (spp == 0) use = false;
