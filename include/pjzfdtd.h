@@ -221,6 +221,19 @@ int32_t pjzfdtd_plan_launch_config(const pjzfdtd_plan* plan, int32_t* tile_y,
                                    int32_t* steps_per_pass, int32_t* kernel,
                                    int32_t* stages);
 
+/* Permittivity of the Yee cell from magnified layer profiles: pjz's
+   `epsilon(layers, interface_positions, magnification, zz,
+   use_simple_averaging)` (src/pjz/_epsilon.py:104-155) on the GPU, so a
+   design -> epsilon -> solve chain stays on the device.  `layers`: device
+   (ll, 2m*xx, 2m*yy) float32 with 1 <= ll <= 16 (m = magnification);
+   `interface_positions`: host, ll - 1 floats, increasing; `out`: device
+   (3, xx, yy, zz) float32.  Stream-ordered, no workspace. */
+int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
+                               int32_t yy, int32_t zz, int32_t magnification,
+                               const float* interface_positions,
+                               int32_t use_simple_averaging, float* out,
+                               void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -4,12 +4,16 @@ Public API (mirrors pjz's ``src/pjz/_field.py``):
   * :class:`SimParams`, :func:`field` -- time-harmonic fields;
   * :func:`scatter` -- scattering values between port modes;
   * :func:`fdtdz` -- drop-in for the ``fdtdz_jax.fdtdz`` engine call;
+  * :func:`epsilon` -- pjz's Yee-cell permittivity rendering
+    (``src/pjz/_epsilon.py``) on the GPU;
   * :class:`engine.Plan` -- the plan/run API over the C ABI.
 """
 
 from ._field import SimParams, field
 from ._fdtdz import LaunchParams, fdtdz
 from ._scatter import scatter
+from ._epsilon import epsilon
 from . import engine
 
-__all__ = ["SimParams", "field", "scatter", "fdtdz", "LaunchParams", "engine"]
+__all__ = ["SimParams", "field", "scatter", "fdtdz", "LaunchParams", "epsilon",
+           "engine"]

@@ -64,6 +64,7 @@ SIGNATURES = {
     "pjzfdtd_batch_workspace_bytes": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "pjzfdtd_batch_run": (_I, [_P, _P, _P, ctypes.c_size_t, _I, _P]),
     "pjzfdtd_batch_destroy": (_I, [_P]),
+    "pjzfdtd_render_epsilon": (_I, [_P, _I, _I, _I, _I, _I, _P, _I, _P, _P]),
 }
 
 _lib = None

@@ -2,6 +2,7 @@
 // translation unit (compiled in parallel) and looked up by the host code.
 #pragma once
 
+#include "render_kernel.cuh"
 #include "stream_kernel.cuh"
 
 namespace pjzfdtd {
@@ -26,5 +27,8 @@ BatchKernel batch2_kernel_ptr();
 inline BatchKernel batch_kernel_ptr(int steps) {
   return steps == 2 ? batch2_kernel_ptr() : batch1_kernel_ptr();
 }
+// Permittivity rendering kernel (kern_render.cu).
+using RenderKernel = void (*)(RenderArgs);
+RenderKernel render_kernel_ptr();
 
 }  // namespace pjzfdtd

@@ -1137,6 +1137,47 @@ int32_t pjzfdtd_batch_destroy(pjzfdtd_batch* batch) {
   return PJZFDTD_OK;
 }
 
+int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
+                               int32_t yy, int32_t zz, int32_t magnification,
+                               const float* interface_positions,
+                               int32_t use_simple_averaging, float* out,
+                               void* stream) {
+  if (!layers || !out) return fail(PJZFDTD_ERR_INVALID, "NULL layers or out");
+  if (ll < 1 || ll > kRenderMaxLayers)
+    return fail(PJZFDTD_ERR_INVALID, "layers must number 1 to %d, got %d",
+                kRenderMaxLayers, ll);
+  if (xx < 1 || yy < 1 || zz < 1 || magnification < 1)
+    return fail(PJZFDTD_ERR_INVALID,
+                "xx, yy, zz and magnification must be positive, got %d, %d, %d, %d",
+                xx, yy, zz, magnification);
+  if (ll > 1 && !interface_positions)
+    return fail(PJZFDTD_ERR_INVALID, "%d interface positions needed", ll - 1);
+  const size_t smem = render_smem_floats(ll, zz) * sizeof(float);
+  const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
+  if (smem > kSmemMax || yblocks > 65535)
+    return fail(PJZFDTD_ERR_INVALID,
+                "zz = %d with %d layers (or yy = %d) exceeds one CTA's reach",
+                zz, ll, yy);
+  RenderArgs a = {};
+  a.layers = layers;
+  a.out = out;
+  a.ll = ll;
+  a.xx = xx;
+  a.yy = yy;
+  a.zz = zz;
+  a.m = magnification;
+  a.simple = use_simple_averaging != 0;
+  for (int i = 0; i + 1 < ll; ++i) a.pos[i] = interface_positions[i];
+  const RenderKernel k = render_kernel_ptr();
+  if (smem > 48 * 1024)
+    CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  const dim3 grid((unsigned)xx, 3, (unsigned)yblocks);
+  k<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  return PJZFDTD_OK;
+}
+
 }  // extern "C"
 
 // Scratch for pjzfdtd_forward_static: a fixed device array, so a caller

@@ -1,0 +1,60 @@
+// Host emulation of render_epsilon_kernel (pjz_gb300/csrc/render_kernel.cuh),
+// for the CPU tests: the kernel's three phases (z occupancy, window
+// statistics, outputs) run for every CTA with the same __host__ __device__
+// functions, every profile read checked against its layer and every output
+// index against the output.  Built with g++ -ffp-contract=off so that its
+// FP32 operations are the kernel's (nvcc -fmad=false).
+#include <stdint.h>
+
+#include <vector>
+
+#define PJZ_RENDER_HOST_CHECK
+#include "render_kernel.cuh"
+
+namespace pjzfdtd {
+size_t g_render_layer_floats = 0;
+int g_render_bad = 0;
+}  // namespace pjzfdtd
+
+using namespace pjzfdtd;
+
+// Returns 0, or 1 when a read or write left its array.
+extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
+                           int m, const float* pos, int simple, float* out) {
+  RenderArgs a = {};
+  a.layers = layers;
+  a.out = out;
+  a.ll = ll;
+  a.xx = xx;
+  a.yy = yy;
+  a.zz = zz;
+  a.m = m;
+  a.simple = simple != 0;
+  for (int i = 0; i + 1 < ll; ++i) a.pos[i] = pos[i];
+  g_render_layer_floats = (size_t)(2 * m * xx) * (2 * m * yy);
+  g_render_bad = 0;
+  const size_t out_floats = (size_t)3 * xx * yy * zz;
+  std::vector<float> sm(render_smem_floats(ll, zz));
+  float* frac = sm.data();
+  float* mid = frac + ll * zz;
+  WindowStats* st = reinterpret_cast<WindowStats*>(mid + ll * zz);
+  for (int c = 0; c < 3; ++c)
+    for (int x = 0; x < xx; ++x)
+      for (int y0 = 0; y0 < yy; y0 += kRenderTileY) {
+        const int ny = yy - y0 < kRenderTileY ? yy - y0 : kRenderTileY;
+        for (int i = 0; i < ll * zz; ++i)
+          render_occupancy(a, c, i / zz, i % zz, &frac[i], &mid[i]);
+        for (int i = 0; i < ny * ll; ++i)
+          st[i] = render_window(a, c, i % ll, x, y0 + i / ll);
+        for (int i = 0; i < ny * zz; ++i) {
+          const int yl = i / zz, z = i - yl * zz;
+          const size_t o = render_out_index(a, c, x, y0 + yl, z);
+          if (o >= out_floats) {
+            g_render_bad = 1;
+            continue;
+          }
+          out[o] = render_value(a, c, st + yl * ll, frac, mid, z);
+        }
+      }
+  return g_render_bad;
+}
