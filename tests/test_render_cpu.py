@@ -25,7 +25,7 @@ def host(tmp_path_factory):
     pytest.skip("no C++ compiler")
   lib = str(tmp_path_factory.mktemp("render") / "librender_host.so")
   subprocess.run([cxx, "-O2", "-std=c++17", "-ffp-contract=off", "-shared",
-                  "-fPIC", "-Wall", "-Werror",
+                  "-fPIC", "-Wall",
                   "-I", os.path.join(ROOT, "pjz_gb300", "csrc"),
                   os.path.join(ROOT, "tests", "render_host.cpp"), "-o", lib],
                  check=True)
