@@ -47,9 +47,12 @@ def _args():
   ap.add_argument("--warmup", type=int, default=3)
   ap.add_argument("--impl", default="native", choices=["native", "reference"])
   ap.add_argument("--workload", default="c1",
-                  choices=["c0", "c1", "c3", "c4", "src-x", "src-y", "src-y6"],
+                  choices=["c0", "c1", "c3", "c4", "src-x", "src-y", "src-y6",
+                           "render"],
                   help="src-*: one-step launches of 512x512x64 with an x-normal, "
-                       "y-normal or 6-column y-normal source box (straggler study)")
+                       "y-normal or 6-column y-normal source box (straggler "
+                       "study); render: permittivity rendering of a 512x512 "
+                       "stack, zz 64")
   ap.add_argument("--batch-n", type=int, default=64, help="c3: problems")
   ap.add_argument("--tune", action="store_true", help="c3: autotune per shape")
   ap.add_argument("--tt", type=int, default=0, help="override time steps")
@@ -555,9 +558,51 @@ def run_source_box(args):
       "launch": p.launch_config()}), flush=True)
 
 
+def run_render(args):
+  """pjz_gb300.epsilon on a 3-layer stack of 512 x 512 cells at 2x
+  magnification, zz 64: W warm-up and K timed renders (CUDA events on the
+  current stream, L2 flushed by a 256 MB write before each), against the
+  algorithmic bytes ll (2m)^2 4 read + 3 zz 4 written per (x, y) column."""
+  import torch
+  import pjz_gb300
+  dev = torch.device("cuda", 0)
+  m, zz, ll, n = 2, 64, 3, 512
+  g = torch.Generator(device=dev).manual_seed(0)
+  layers = 2.085 + 10.165 * torch.rand((ll, 2 * m * n, 2 * m * n), device=dev,
+                                        generator=g)
+  pos = np.array([28.5, 35.25], np.float32)
+  out = torch.empty((3, n, n, zz), device=dev)
+  flush = torch.empty(64 << 20, device=dev)
+  for _ in range(max(args.warmup, 3)):
+    pjz_gb300.epsilon(layers, pos, m, zz, out=out)
+  times = []
+  for _ in range(args.steps):
+    flush.fill_(1.0)
+    e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+    e0.record()
+    pjz_gb300.epsilon(layers, pos, m, zz, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    times.append(e0.elapsed_time(e1) / 1e3)
+  t = statistics.median(times)
+  nbytes = n * n * (ll * (2 * m) ** 2 * 4 + 3 * zz * 4)
+  peak, kind = _peaks()
+  gbs = nbytes / t / 1e9
+  print(json.dumps({
+      "workload": "render 512x512 cells, 3 layers, 2x, zz 64", "ms": t * 1e3,
+      "algorithmic_bytes": nbytes, "achieved_gbs": gbs,
+      "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak,
+                   "unit": "GB/s", "frac": gbs / peak, "peak_kind": kind},
+      "steps": args.steps, "warmup": max(args.warmup, 3),
+      "timing": "median of CUDA-event times, L2 flushed before each"}),
+      flush=True)
+
+
 if __name__ == "__main__":
   a = _args()
-  if a.workload in SOURCE_BOXES:
+  if a.workload == "render":
+    run_render(a)
+  elif a.workload in SOURCE_BOXES:
     run_source_box(a)
   elif a.impl == "reference":
     run_reference(a)
