@@ -10,6 +10,7 @@ the product's mirror of the same helpers (``pjz_gb300/field.py``).
 
 import json
 import os
+import zlib
 
 import numpy as np
 import pytest
@@ -273,3 +274,39 @@ def test_reciprocity_with_cpml_stretch():
     assert abs(ratio - 1) > 0.2
     got = (ph @ zb_from_xa) / (ph @ xa_from_zb)
     assert abs(got - ratio) < 2e-6 * abs(ratio), (w, got, ratio)
+
+
+@pytest.mark.parametrize("orient", ["x", "y", "z"])
+@pytest.mark.parametrize("pml,kinf", [((0, 0), False), ((3, 4), False),
+                                       ((0, 5), False), ((2, 2), True)])
+@pytest.mark.parametrize("full_region", [False, True])
+def test_c_oracle_matches_numpy_fp64_variants(orient, pml, kinf, full_region):
+  """The C oracle and the independent NumPy transcription agree (FP64) for
+  every source orientation, z-PML layout (none, asymmetric, one-sided,
+  kappa = inf) and epsilon region (offset inside the domain or the whole
+  domain): snapshots and final fields."""
+  rng = np.random.default_rng(zlib.crc32(repr((orient, pml, kinf, full_region)).encode()))
+  X, Y, Z, tt = 12, 10, 16, 50
+  if full_region:
+    eps, offset = rng.uniform(1, 4, (3, X, Y, Z)), (0, 0, 0)
+  else:
+    eps, offset = rng.uniform(1, 4, (3, X - 4, Y - 4, Z - 6)), (2, 2, 3)
+  sf = {"x": (rng.normal(size=(2, 1, Y, Z)), 5),
+        "y": (rng.normal(size=(2, X, 1, Z)), 4),
+        "z": (rng.normal(size=(2, 2, X, Y, 1)), 7)}[orient]
+  org, shp, prof = oracle.plane_source_box(sf[0].astype(np.float32), sf[1], (X, Y, Z))
+  sig = (pjz_ref.pml_sigma(pml, Z, 0.5, 1.3) if sum(pml) else
+         np.zeros((Z, 2))).astype(np.float32)
+  kappa = np.full_like(sig, np.inf) if kinf else np.ones_like(sig)
+  kw = dict(eps=eps.astype(np.float32), offset=offset,
+            mask=pjz_ref.absorption_mask(X, Y, 2, 0.05).astype(np.float32),
+            kappa=kappa, sigma=sig, alpha=np.full_like(sig, 0.05), dt=0.5, tt=tt,
+            pml_widths=pml, source_origin=org, source_profile=prof,
+            waveform=rng.normal(size=(tt, 2)).astype(np.float32),
+            output_steps=(30, 50, 5))
+  c = oracle.run(**kw, precision="f64", fields=np.zeros((6, X, Y, Z)))
+  snaps, fields = yee_numpy.run(**kw)
+  scale = np.abs(fields).max()
+  assert scale > 0 and np.abs(snaps).max() > 0
+  np.testing.assert_allclose(c["out"], snaps, rtol=0, atol=1e-12 * scale)
+  np.testing.assert_allclose(c["fields"], fields, rtol=0, atol=1e-12 * scale)
