@@ -130,3 +130,21 @@ def test_fp64_oracle_adjoint_matches_finite_differences():
   fd = np.array(fd)
   ad = np.array([grad[p] for p in pts])
   assert np.linalg.norm(fd - ad) / np.linalg.norm(fd) < 1e-3, (fd, ad)
+
+
+@pytest.mark.parametrize("pml,kappa_val,alpha_val", [
+    ((4, 4), 1.0, 0.05), ((3, 5), 2.0, 0.0), ((0, 6), 1.5, 0.1), ((4, 4), np.inf, 0.0)])
+def test_cpml_stretch_matches_oracle(pml, kappa_val, alpha_val):
+  """The product's CPML stretch (used by the S-matrix unit adjoints) equals
+  the oracle's, which the time-domain reciprocity KAT pins: kappa != 1,
+  alpha != 0, one-sided slabs and kappa = inf."""
+  from oracle import adjoint as oadj
+  from pjz_gb300 import _adjoint
+  Z = 16
+  sig = pjz_ref.pml_sigma(pml, Z, 0.5, 1.3)
+  kap = np.full_like(sig, kappa_val)
+  alp = np.full_like(sig, alpha_val)
+  om = np.array([0.12, 0.16215, 0.3])
+  got = _adjoint.cpml_stretch(om, 0.5, kap, sig, alp, pml)
+  want = oadj.stretch(om, 0.5, kap, sig, alp, pml)
+  np.testing.assert_allclose(got, want, rtol=1e-12, atol=0)
