@@ -18,8 +18,14 @@ ring depths, segments, source boxes and thread counts the test checks that
   update needs, or a zero row outside the domain;
 * no float is written by one thread and touched by another between two
   barriers;
-* every float a bulk store reads was written for the plane it stores, and
-  every output row of the launch is stored exactly once.
+* every float a bulk store reads was written for the plane it stores, both
+  when the store may start (after the plane's E phase) and when it may
+  still be reading (until the compute warps wait on it two planes later),
+  and every output row of the launch is stored exactly once.
+
+The one-step replay also takes the number of new-H buffers and of barriers
+per plane as parameters, so that a change to that protocol is checked here
+before it is made in the kernel.
 
 It mirrors the kernels' index arithmetic line for line (the shared helpers
 `h_pair` / `e_pair` follow the kernels' helpers of the same names); a
@@ -227,12 +233,17 @@ def pml_columns(Z, plo, phi):
 
 
 def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
-                 plant=None):
+                 plant=None, hbuf=2, barriers=2):
   """Replays CTA (tile, seg) of yee_stream_kernel; returns its Smem or None
   when the host refuses the tile.  `cover[x, y]` counts the rows stored.
   `plant` puts a known mistake into the replay (for the tests that show the
   model catches it): "slot" reads plane x+1 from one ring slot too far,
-  "moff" drops the absorber window offset."""
+  "moff" drops the absorber window offset.  `hbuf` (new-H buffers) and
+  `barriers` (named barriers per plane) are 2 and 2 in the kernel; other
+  values replay a candidate protocol: with one barrier the E phase of plane
+  x shares its interval with the H phase of plane x + 1.  The producer's
+  stores of plane x are checked both right after its E phase and at the
+  latest moment they may read, just before plane x + 2's wait on them."""
   P = plo + phi
   Pp = r4(P)
   Yp = r4(Y)
@@ -245,7 +256,7 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   s_off = p_off + 4 * RH * Pp
 
   def smem_bytes(sw):
-    floats = S * (s_off + sw) + 2 * 3 * RH * Z + 2 * 3 * TY * Z + 2 * 4 * TY * Pp
+    floats = S * (s_off + sw) + hbuf * 3 * RH * Z + 2 * 3 * TY * Z + 2 * 4 * TY * Pp
     return floats * 4 + (2 * S + 2) * 8 + 16
 
   if smem_bytes(0) > SMEM_BUDGET:
@@ -260,7 +271,7 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   SR = sw > 0
   stage = s_off + sw
   hn = S * stage
-  en = hn + 2 * 3 * RH * Z
+  en = hn + hbuf * 3 * RH * Z
   pn = en + 2 * 3 * TY * Z
   end = pn + 2 * 4 * TY * Pp
   RHZ, REZ = RH * Z, RE * Z
@@ -306,14 +317,27 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
     fill(x0 + nfill, nfill, x0 + nfill < xe)
     nfill += 1
 
+  def stores(x, hcur, ecur, pcur):
+    for c in range(3):
+      sm.stored("H out", hcur + c * RHZ + Z, rows_tag(H + c, 1, x, y0, hy_hi, Z))
+      sm.stored("E out", ecur + c * TY * Z, rows_tag(E + c, 1, x, y0, hy_hi, Z))
+    if Pp:
+      col = np.tile(np.arange(Pp) < P, nrows)
+      for c in range(4):
+        sm.stored("psi out", pcur + c * TY * Pp,
+                  rows_tag(PSI + c, 1, x, y0, hy_hi, Pp), col)
+
+  pending = {}  # plane index k -> its stores, checked again before k + 2
   slot, slot1 = 0, (1 if S > 1 else 0)
   for x in range(x0, xe):
     k = x - x0
     b = k & 1
+    if k - 2 in pending:
+      stores(*pending.pop(k - 2))
     st = slot * stage
     Es, E1 = st + e_off, slot1 * stage + e_off
     Hs, Cs, Ms, Ps = st + h_off, st + c_off, st + m_off + moff, st + p_off
-    hcur, hprev = hn + b * 3 * RHZ, hn + (b ^ 1) * 3 * RHZ
+    hcur, hprev = hn + (k % hbuf) * 3 * RHZ, hn + ((k - 1) % hbuf) * 3 * RHZ
     ecur, pcur = en + b * 3 * TY * Z, pn + b * 4 * TY * Pp
     po_hi = pcur + 4 * TY * Pp
     wr = x >= xs
@@ -391,23 +415,21 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
       for c in range(3):
         sm.write("E out", ecur + c * TY * Z + ic, thr, tag(E + c, 1, x, y), ecur,
                  ecur + 3 * TY * Z, 2)
-      sm.end("E phase")
+      if barriers == 2:
+        sm.end("E phase")
 
     # Producer after done[slot]: bulk stores of plane x, then the refill.
     if wr:
-      for c in range(3):
-        sm.stored("H out", hcur + c * RHZ + Z, rows_tag(H + c, 1, x, y0, hy_hi, Z))
-        sm.stored("E out", ecur + c * TY * Z, rows_tag(E + c, 1, x, y0, hy_hi, Z))
-      if Pp:
-        col = np.tile(np.arange(Pp) < P, nrows)
-        for c in range(4):
-          sm.stored("psi out", pcur + c * TY * Pp,
-                    rows_tag(PSI + c, 1, x, y0, hy_hi, Pp), col)
+      stores(x, hcur, ecur, pcur)
+      pending[k] = (x, hcur, ecur, pcur)
       cover[x, y0:hy_hi] += 1
     if x0 + nfill <= xlast:
       fill(x0 + nfill, slot, x0 + nfill < xe)
       nfill += 1
     slot, slot1 = slot1, (slot1 + (2 if plant == "slot" else 1)) % S
+  sm.end("last plane")
+  for args in pending.values():
+    stores(*args)
   return sm
 
 
@@ -622,10 +644,11 @@ def run_grid(cta, X, Y, TY, seg_x, cover_shape):
   return reads, bad, cover
 
 
-def one_step(X, Y, Z, plo, phi, TY, S, seg_x, ncomp, src, plant=None):
+def one_step(X, Y, Z, plo, phi, TY, S, seg_x, ncomp, src, plant=None, hbuf=2,
+             barriers=2):
   def cta(tile, seg, cover):
     return one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src,
-                        cover, plant)
+                        cover, plant, hbuf, barriers)
   return run_grid(cta, X, Y, TY, seg_x, (X, Y))
 
 
@@ -737,3 +760,25 @@ def test_model_flags_a_race():
   sm.read("r", [4], 1, 1, False, 0, 16)
   sm.end("phase")
   assert any(b[1] == "race" for b in sm.bad)
+
+
+def test_one_barrier_protocol_needs_three_h_buffers():
+  """A candidate change to the one-step kernel, checked before it is made.
+  Dropping the barrier after the E phase lets plane x's E phase overlap
+  plane x + 1's H phase.  With two new-H buffers that overlap is a race
+  (H(x + 1) overwrites H(x - 1), which E(x) still reads).  With three
+  buffers the replay is clean, including the producer's delayed stores.
+  The third buffer fits the production tile (zz 64, tile_y 14, 4 ring
+  stages, 16-cell PML) within the host's shared-memory budget."""
+  cases = [(9, 20, 16, 2, 2, 5, 3, 3, 32, (2, 0, 0, 2, 20, 16, 2)),
+           (8, 11, 32, 1, 3, 5, 4, 8, 192, (0, 0, 1, 8, 11, 1, 4)),
+           (6, 13, 64, 2, 2, 14, 4, 6, 480, None)]
+  for c in cases:
+    assert one_step(*c, hbuf=2, barriers=2)[1] == []
+    assert one_step(*c, hbuf=3, barriers=1)[1] == []
+    assert any(b[3] == "race" for b in one_step(*c, hbuf=2, barriers=1)[1])
+  RE, RH, TY, Z, Pp, S = 16, 15, 14, 64, 16, 4
+  stage = 3 * RE * Z + 3 * RH * Z + 3 * TY * Z + 3 * (r4(TY) + 8) + 4 * RH * Pp
+  for hbuf, fits in ((2, True), (3, True), (4, False)):
+    floats = S * stage + hbuf * 3 * RH * Z + 2 * 3 * TY * Z + 2 * 4 * TY * Pp
+    assert (floats * 4 + (2 * S + 2) * 8 + 16 <= SMEM_BUDGET) == fits
