@@ -782,3 +782,30 @@ def test_one_barrier_protocol_needs_three_h_buffers():
   for hbuf, fits in ((2, True), (3, True), (4, False)):
     floats = S * stage + hbuf * 3 * RH * Z + 2 * 3 * TY * Z + 2 * 4 * TY * Pp
     assert (floats * 4 + (2 * S + 2) * 8 + 16 <= SMEM_BUDGET) == fits
+
+
+def test_random_shapes():
+  """Seeded random launches beyond the grid above: any zz that is a
+  multiple of 4 up to 64, tile heights to 29, ring depths 2-8, uneven PML
+  slabs, both thread counts, every source box; one- and two-step."""
+  import random
+  rng = random.Random(1)
+  done = 0
+  while done < 30:
+    Z = rng.choice(range(4, 68, 4))
+    X, Y = rng.randint(2, 9), rng.randint(1, 40)
+    plo, phi = rng.randint(0, min(4, Z // 4)), rng.randint(0, min(4, Z // 4))
+    TY, S, seg = rng.randint(1, min(Y, 29)), rng.randint(2, 8), rng.randint(1, X)
+    nc = rng.choice([host_ncomp(Z, TY), min_ncomp(Z)])
+    src = source_box(rng.randint(0, 5), X, Y, Z)
+    res = one_step(X, Y, Z, plo, phi, TY, S, seg, nc, src)
+    if res is not None:
+      assert not res[1] and (res[2] == 1).all(), (X, Y, Z, plo, phi, TY, S, seg,
+                                                   nc, src, res[1][:2])
+      done += 1
+    TY2 = rng.randint(1, min(Y, 14))
+    nc2 = rng.choice([host_ncomp2(Z, TY2), min_ncomp(Z)])
+    res = two_step(X, Y, Z, plo, phi, TY2, rng.randint(2, 3), seg, nc2)
+    if res is not None:
+      assert not res[1] and (res[2] == 1).all(), (X, Y, Z, plo, phi, TY2, seg,
+                                                   nc2, res[1][:2])
