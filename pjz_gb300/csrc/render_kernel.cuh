@@ -21,8 +21,13 @@
 // One CTA per (x, component, block of kRenderTileY y cells): it tabulates
 // the z occupancy of its component's cells and the window statistics of its
 // y cells in shared memory, then writes its (y, z) outputs with z fastest.
-// FP32 throughout; the per-cell functions are __host__ __device__ so that a
-// host emulation of the block loop checks the same code on the CPU.
+// A z cell that lies wholly inside one layer (its fraction exactly 1, all
+// others exactly 0) has the same value at every such z of a column: it is
+// computed once per (y, layer) and copied, and only the cells an interface
+// cuts take the full mix.  Both give the same floats (the full mix adds
+// exact zeros to that layer's terms).  FP32 throughout; the per-cell
+// functions are __host__ __device__ so that a host emulation of the block
+// loop checks the same code on the CPU.
 #pragma once
 
 #include <math.h>
@@ -67,10 +72,11 @@ PJZ_HD float render_load(const float* layer, size_t i) { return layer[i]; }
 
 PJZ_HD int render_imax(int a, int b) { return a > b ? a : b; }
 
-// Shared-memory floats of one CTA: occupancy [2][ll][zz], statistics
-// [kRenderTileY][ll] of 4 floats.
+// Shared-memory floats of one CTA: occupancy [2][ll][zz], the layer that
+// fills each z cell [zz] (int, -1 when an interface cuts it), statistics
+// [kRenderTileY][ll] of 4 floats, one-layer values [kRenderTileY][ll].
 PJZ_HD size_t render_smem_floats(int ll, int zz) {
-  return 2 * (size_t)ll * zz + 4 * (size_t)kRenderTileY * ll;
+  return 2 * (size_t)ll * zz + zz + 5 * (size_t)kRenderTileY * ll;
 }
 
 // Filled fraction of z cell `z` of component `c` by layer `l`, and the
@@ -115,6 +121,17 @@ PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int l, int x, int y
   return w;
 }
 
+// The value from the fraction-weighted sums over the layers.
+PJZ_HD float render_mix(const RenderArgs& a, int c, float avg, float inv,
+                        float gx, float gy, float gz) {
+  if (a.simple) return avg;
+  gz = 12.0f * gz;  // first moment over the unit cell's second moment 1/12
+  const float norm = gx * gx + gy * gy + gz * gz;
+  const float g = c == 0 ? gx : (c == 1 ? gy : gz);
+  const float p = norm == 0.0f ? 0.0f : g * g / norm;
+  return 1.0f / (p * inv + (1.0f - p) / avg);
+}
+
 // Value of component `c` at z from the window statistics of its (x, y)
 // (st[l]) and the occupancy of its z cells (frac / mid [l * zz + z]).
 PJZ_HD float render_value(const RenderArgs& a, int c, const WindowStats* st,
@@ -128,12 +145,21 @@ PJZ_HD float render_value(const RenderArgs& a, int c, const WindowStats* st,
     gy += st[l].gy * f;
     gz += st[l].mean * f * mid[l * a.zz + z];
   }
-  if (a.simple) return avg;
-  gz = 12.0f * gz;  // first moment over the unit cell's second moment 1/12
-  const float norm = gx * gx + gy * gy + gz * gz;
-  const float g = c == 0 ? gx : (c == 1 ? gy : gz);
-  const float p = norm == 0.0f ? 0.0f : g * g / norm;
-  return 1.0f / (p * inv + (1.0f - p) / avg);
+  return render_mix(a, c, avg, inv, gx, gy, gz);
+}
+
+// Value of a z cell that one layer fills: render_value with that layer's
+// fraction 1, midpoint offset 0 and every other fraction 0 (each sum then
+// holds that layer's term alone, and the z moment +0).
+PJZ_HD float render_interior(const RenderArgs& a, int c, const WindowStats& w) {
+  return render_mix(a, c, 0.f + w.mean, 0.f + w.inv, 0.f + w.gx, 0.f + w.gy, 0.f);
+}
+
+// The layer whose fraction of z cell `z` is exactly 1, else -1.
+PJZ_HD int render_owner(const RenderArgs& a, const float* frac, int z) {
+  for (int l = 0; l < a.ll; ++l)
+    if (frac[l * a.zz + z] == 1.0f) return l;
+  return -1;
 }
 
 PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) {
@@ -149,16 +175,24 @@ __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a)
   const int ny = min(kRenderTileY, a.yy - y0);
   float* frac = rsm;
   float* mid = frac + a.ll * a.zz;
-  WindowStats* st = reinterpret_cast<WindowStats*>(mid + a.ll * a.zz);
-  for (int i = threadIdx.x; i < a.ll * a.zz; i += blockDim.x)
-    render_occupancy(a, c, i / a.zz, i % a.zz, &frac[i], &mid[i]);
-  for (int i = threadIdx.x; i < ny * a.ll; i += blockDim.x)
+  int* owner = reinterpret_cast<int*>(mid + a.ll * a.zz);
+  WindowStats* st = reinterpret_cast<WindowStats*>(owner + a.zz);
+  float* ival = reinterpret_cast<float*>(st + kRenderTileY * a.ll);
+  for (int z = threadIdx.x; z < a.zz; z += blockDim.x) {
+    for (int l = 0; l < a.ll; ++l)
+      render_occupancy(a, c, l, z, &frac[l * a.zz + z], &mid[l * a.zz + z]);
+    owner[z] = render_owner(a, frac, z);
+  }
+  for (int i = threadIdx.x; i < ny * a.ll; i += blockDim.x) {
     st[i] = render_window(a, c, i % a.ll, x, y0 + i / a.ll);
+    ival[i] = render_interior(a, c, st[i]);
+  }
   __syncthreads();
   for (int i = threadIdx.x; i < ny * a.zz; i += blockDim.x) {
     const int yl = i / a.zz, z = i - yl * a.zz;
+    const int o = owner[z];
     a.out[render_out_index(a, c, x, y0 + yl, z)] =
-        render_value(a, c, st + yl * a.ll, frac, mid, z);
+        o >= 0 ? ival[yl * a.ll + o] : render_value(a, c, st + yl * a.ll, frac, mid, z);
   }
 }
 #endif

@@ -1,9 +1,10 @@
 // Host emulation of render_epsilon_kernel (pjz_gb300/csrc/render_kernel.cuh),
-// for the CPU tests: the kernel's three phases (z occupancy, window
-// statistics, outputs) run for every CTA with the same __host__ __device__
-// functions, every profile read checked against its layer and every output
-// index against the output.  Built with g++ -ffp-contract=off so that its
-// FP32 operations are the kernel's (nvcc -fmad=false).
+// for the CPU tests: the kernel's three phases (z occupancy and filling
+// layer, window statistics and one-layer values, outputs) run for every CTA
+// with the same __host__ __device__ functions and shared-memory carving,
+// every profile read checked against its layer and every output index
+// against the output.  Built with g++ -ffp-contract=off so that its FP32
+// operations are the kernel's (nvcc -fmad=false).
 #include <stdint.h>
 
 #include <vector>
@@ -37,15 +38,23 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   std::vector<float> sm(render_smem_floats(ll, zz));
   float* frac = sm.data();
   float* mid = frac + ll * zz;
-  WindowStats* st = reinterpret_cast<WindowStats*>(mid + ll * zz);
+  int* owner = reinterpret_cast<int*>(mid + ll * zz);
+  WindowStats* st = reinterpret_cast<WindowStats*>(owner + zz);
+  float* ival = reinterpret_cast<float*>(st + kRenderTileY * ll);
+  if (ival + kRenderTileY * ll != sm.data() + sm.size()) return 1;  // carving
   for (int c = 0; c < 3; ++c)
     for (int x = 0; x < xx; ++x)
       for (int y0 = 0; y0 < yy; y0 += kRenderTileY) {
         const int ny = yy - y0 < kRenderTileY ? yy - y0 : kRenderTileY;
-        for (int i = 0; i < ll * zz; ++i)
-          render_occupancy(a, c, i / zz, i % zz, &frac[i], &mid[i]);
-        for (int i = 0; i < ny * ll; ++i)
+        for (int z = 0; z < zz; ++z) {
+          for (int l = 0; l < ll; ++l)
+            render_occupancy(a, c, l, z, &frac[l * zz + z], &mid[l * zz + z]);
+          owner[z] = render_owner(a, frac, z);
+        }
+        for (int i = 0; i < ny * ll; ++i) {
           st[i] = render_window(a, c, i % ll, x, y0 + i / ll);
+          ival[i] = render_interior(a, c, st[i]);
+        }
         for (int i = 0; i < ny * zz; ++i) {
           const int yl = i / zz, z = i - yl * zz;
           const size_t o = render_out_index(a, c, x, y0 + yl, z);
@@ -53,7 +62,9 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
             g_render_bad = 1;
             continue;
           }
-          out[o] = render_value(a, c, st + yl * ll, frac, mid, z);
+          const int w = owner[z];
+          out[o] = w >= 0 ? ival[yl * ll + w]
+                          : render_value(a, c, st + yl * ll, frac, mid, z);
         }
       }
   return g_render_bad;
