@@ -59,6 +59,8 @@ def _args():
   ap.add_argument("--cpu-seconds", type=float, default=12.0)
   ap.add_argument("--no-e2e", action="store_true")
   ap.add_argument("--no-cpu", action="store_true")
+  ap.add_argument("--no-batched", action="store_true",
+                  help="c1: skip the batched c4 S-matrix gradient leg")
   ap.add_argument("--kernel", type=int, default=0,
                   help="0 auto, 1 register-marching, 2 streamed")
   ap.add_argument("--stages", type=int, default=0)
@@ -365,6 +367,11 @@ def run_native(args):
   if rank == 0 and not args.no_cpu:
     cpu = cpu_baseline(wl, args.cpu_seconds)
 
+  batched = None
+  if args.workload == "c1" and not args.no_batched:
+    batched = (batched_c4(local, _clock_path(f"c4_{rank}")) if world == 1 else
+               {"skipped": "the c4 leg runs on one GPU (replicas only)"})
+
   if rank == 0:
     cfg = plan.launch_config()
     line = {
@@ -380,6 +387,7 @@ def run_native(args):
                    "parallelism": "replicas" if world > 1 else "single",
                    "launch": cfg},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+        "batched": batched,
         # per solve: the step launches of its schedule, the cb and absorber
         # set-up kernels and one record pass per sample step.
         "gpu_launches": args.steps * (plan.step_launches() + 2 + plan.num_samples),
@@ -388,6 +396,44 @@ def run_native(args):
     print(json.dumps(line), flush=True)
   if world > 1:
     torch.distributed.destroy_process_group()
+
+
+def batched_c4(device_index, clock_path):
+  """The batched half of the metric: config c4 (8-port S-matrix on
+  1024x1024x64, 8 forward + 8 unit-adjoint solves, 12000 steps, 3
+  frequencies) as one graph-captured batched launch against the serial
+  loop of the same 16 solves (pjz's per-port loop), in gradients per
+  second.  One batched warm-up run (graph capture, workspaces, clocks),
+  then one serial and one batched run, timed back to back."""
+  import torch
+  from pjz_gb300 import smatrix
+  dev = torch.device("cuda", device_index)
+  s = smatrix.SMatrixSolver(smatrix.build_c4(), device=dev)
+  t0 = time.perf_counter()
+  s.run_batched(graph=True)
+  torch.cuda.synchronize()
+  t_warm = time.perf_counter() - t0
+  for p in s.plans:  # the serial loop's workspaces, outside the timing
+    p.workspace(dev)
+  t_batch, t_serial, clk = _alternate(lambda: s.run_batched(graph=True),
+                                      s.run_serial, 1, clock_path)
+  s.batch.check_status()
+  S, L, grad = s.results()
+  cells = s.cell_updates
+  return {"value": 1.0 / t_batch, "unit": "grads/s",
+          "workload": "c4 8-port S-matrix gradient, 1024x1024x64, 8 forward + "
+                      "8 unit-adjoint solves, 12000 steps, 3 frequencies",
+          "gcell_updates_per_s": cells / t_batch / 1e9,
+          "seconds_per_grad": t_batch,
+          "serial_loop": {"value": 1.0 / t_serial, "unit": "grads/s",
+                          "gcell_updates_per_s": cells / t_serial / 1e9,
+                          "seconds_per_grad": t_serial},
+          "speedup": t_serial / t_batch,
+          "objective": float(L), "grad_finite": bool(torch.isfinite(grad).all()),
+          "timing": f"one batched warm-up run ({t_warm:.1f} s incl. graph "
+                    "capture), then one serial and one batched run timed "
+                    "with the host clock around a device synchronise",
+          "clocks": clk}
 
 
 def _alternate(fa, fb, reps, clock_path):

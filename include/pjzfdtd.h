@@ -197,15 +197,24 @@ int32_t pjzfdtd_batch_destroy(pjzfdtd_batch* batch);
    given no scratch operand), or a real-time loop that must not risk the
    implicit device synchronisation cudaMalloc/cudaFree can cause.  Plans
    whose workspace (pjzfdtd_plan_workspace_bytes) exceeds 64 MiB are
-   rejected with PJZFDTD_ERR_WORKSPACE.  The first call on a device resolves
-   the array's device address (cudaGetSymbolAddress) with that device
-   current; make that first call before any stream capture.  All calls on a
-   device share the one array and it keeps the last call's contents (each
-   solve re-initialises what it needs); calls that overlap on the GPU, for
-   example on two streams, race on it.  Otherwise it behaves as
-   pjzfdtd_forward (same plan, buffers and results). */
+   rejected with PJZFDTD_ERR_WORKSPACE.  Each call made outside a stream
+   capture looks up the array's device address (cudaGetSymbolAddress) with
+   the device current and caches it per device; a call during a capture
+   uses the cached address, so make one call on each device before any
+   stream capture.  All calls on a device share the one array and it keeps
+   the last call's contents (each solve re-initialises what it needs);
+   calls that overlap on the GPU, for example on two streams, race on it.
+   Otherwise it behaves as pjzfdtd_forward (same plan, buffers and
+   results). */
 int32_t pjzfdtd_forward_static(pjzfdtd_plan* plan,
                                const pjzfdtd_buffers* buffers, void* stream);
+
+/* pjzfdtd_plan_status for solves run by pjzfdtd_forward_static, whose status
+   word lives in the library's static array rather than a caller workspace:
+   PJZFDTD_ERR_TIMEOUT if a bounded device-side wait of the work queued on
+   `stream` gave up (the word is then cleared), PJZFDTD_OK otherwise.
+   Synchronises `stream`.  No counterpart in the reference. */
+int32_t pjzfdtd_forward_static_status(pjzfdtd_plan* plan, void* stream);
 
 /* Reads (and clears) the device status word of `workspace` after the work
    queued on `stream` so far: PJZFDTD_ERR_TIMEOUT if a bounded device-side

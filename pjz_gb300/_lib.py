@@ -58,6 +58,7 @@ SIGNATURES = {
     "pjzfdtd_plan_launch_config": (_I, [_P] + [ctypes.POINTER(_I)] * 6),
     "pjzfdtd_plan_status": (_I, [_P, _P, ctypes.c_size_t, _P]),
     "pjzfdtd_forward_static": (_I, [_P, ctypes.POINTER(Buffers), _P]),
+    "pjzfdtd_forward_static_status": (_I, [_P, _P]),
     "pjzfdtd_plan_set_monitors": (_I, [_P, _I, _P]),
     "pjzfdtd_plan_output_floats": (_I, [_P, ctypes.POINTER(ctypes.c_size_t)]),
     "pjzfdtd_batch_create": (_I, [_P, _I, ctypes.POINTER(_P)]),

@@ -1,0 +1,428 @@
+// Lean streamed Yee step kernel for sm_103a (one time step per launch).
+//
+// Same data movement as yee_stream_kernel (stream_kernel.cuh): a producer
+// warp fills a ring of shared-memory slots with bulk copies of the x-plane
+// tile pieces (E rows -1..TY, H rows -1..TY-1, coefficient rows, absorber
+// row, z-PML state rows) `stages` planes ahead, and bulk-stores the results
+// from staging buffers; the shared-memory layout (StreamGeom) and the
+// producer's copies are those of the streamed kernel.  What differs is the
+// compute side, written for few instructions per cell-update:
+//
+//  * zz and tile_y are compile-time, so every shared-memory offset of a
+//    thread is fixed before the plane loop;
+//  * a compute thread owns one z-quad (4 adjacent z cells, 128-bit shared
+//    accesses) of one buffer row for the whole launch: in the H phase row
+//    rH (y = y0 - 1 + rH), in the E phase tile row rH (y = y0 + rH);
+//  * quads inside the z-PML slabs (the slab widths must be multiples of 4)
+//    belong to their own warps, which carry the CPML state; the other warps
+//    never branch on it;
+//  * the source current is added only on planes the source box crosses
+//    (a plane-uniform test), from global memory as in the streamed kernel.
+//
+// Per cell the arithmetic is the explicit round-to-nearest FP32 sequence of
+// the streamed kernel and of the CPU oracle, so results are bit-identical.
+// Barriers and bounded waits follow the streamed kernel's protocol.
+#pragma once
+
+#include "stream_kernel.cuh"
+#include "kernel_table.cuh"
+
+namespace pjzfdtd {
+
+// Quads per row outside / inside the z-PML slabs and the warps that hold
+// one item each for the tile_y + 1 rows of the H phase.
+__host__ __device__ inline int lean_quads_interior(int Z, int plo, int phi) {
+  return (Z - plo - phi) / 4;
+}
+__host__ __device__ inline int lean_quads_pml(int plo, int phi) {
+  return (plo + phi) / 4;
+}
+__host__ __device__ inline int lean_warps_interior(int Z, int ty, int plo, int phi) {
+  return ((ty + 1) * lean_quads_interior(Z, plo, phi) + 31) / 32;
+}
+__host__ __device__ inline int lean_warps_pml(int ty, int plo, int phi) {
+  return ((ty + 1) * lean_quads_pml(plo, phi) + 31) / 32;
+}
+
+__device__ __forceinline__ float4 lds4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+__device__ __forceinline__ void sts4(float* p, const float v[4]) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+__device__ __forceinline__ void unpack4(const float4 v, float o[4]) {
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+}
+
+// One CTA of the lean kernel: tile `tile` of y rows, segment `seg` of x
+// planes.  ZC / TYC: zz and tile_y (compile-time).
+template <int ZC, int TYC>
+__device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int seg,
+                                          float* sm) {
+  constexpr int Z = ZC, TY = TYC;
+  constexpr int RE = TY + 2, RH = TY + 1;
+  constexpr int REZ = RE * Z, RHZ = RH * Z, TYZ = TY * Z;
+  const StepArgs& a = sa.s;
+  const int X = a.X, Y = a.Y;
+  const int S = sa.stages;
+  const StreamGeom g(TY, Z, a.plo + a.phi, 0);
+  const int Pp = g.Pp;
+  float* hn = sm + (size_t)S * g.stage;   // [2][3][RH*Z]
+  float* en = hn + g.hn_floats();         // [2][3][TY*Z]
+  float* pn = en + g.en_floats();         // [2][4][TY*Pp]
+  uint64_t* full = reinterpret_cast<uint64_t*>(pn + g.pn_floats());
+  uint64_t* done = full + S;
+  uint64_t* freeb = done + S;
+  __shared__ int abort_flag;
+
+  const int tid = threadIdx.x;
+  const int ncomp = blockDim.x - 32;
+  const int nwarps = ncomp >> 5;
+  const bool producer = tid >= ncomp;
+  const int y0 = tile * TY;
+  const int xs = seg * a.seg_x;
+  const int xe = min(X, xs + a.seg_x);
+  const int x0 = xs > 0 ? xs - 1 : 0;
+  const int xlast = min(xe, X - 1);  // last plane whose E is read
+  const long long N = a.N;
+  const long long YZ = (long long)Y * Z;
+  const long long PXY = (long long)X * Y * Pp;
+  const int ey_lo = max(y0 - 1, 0), ey_hi = min(y0 + TY + 1, Y);
+  const int hy_hi = min(y0 + TY, Y);
+  const int nrows = hy_hi - y0;
+  const int erow0 = ey_lo - (y0 - 1);
+  const int ma = y0 & ~3;
+  const int mb = min(round4(y0 + TY), sa.Yp);
+  const int moff = y0 - ma;
+
+  if (tid == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&done[s], nwarps);
+    }
+    mbar_init(&freeb[0], 1);
+    mbar_init(&freeb[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  for (size_t i = tid; i < (size_t)S * g.stage + g.hn_floats() + g.en_floats() +
+                               g.pn_floats();
+       i += blockDim.x)
+    sm[i] = 0.f;
+  fence_async_smem();
+  __syncthreads();
+
+  if (producer) {
+    if ((tid & 31) != 0) return;
+    // ---------------- producer (one lane) ----------------
+    auto fill = [&](int xp, int slot, bool fullp) {
+      float* st = sm + (size_t)slot * g.stage;
+      const uint32_t eb = (uint32_t)((ey_hi - ey_lo) * Z * 4);
+      const uint32_t hb = (uint32_t)((hy_hi - ey_lo) * Z * 4);
+      const uint32_t cbb = (uint32_t)(nrows * Z * 4);
+      const uint32_t mbb = (uint32_t)((mb - ma) * 4);
+      const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
+      const uint32_t total = sa.stall_bytes + 3 * eb +
+          (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
+      mbar_expect_tx(&full[slot], total);
+      const long long base = (long long)xp * YZ;
+      for (int c = 0; c < 3; ++c)
+        bulk_g2s(st + g.e_off + c * REZ + erow0 * Z,
+                 a.fin + c * N + base + (long long)ey_lo * Z, eb, &full[slot]);
+      if (!fullp) return;
+      for (int c = 0; c < 3; ++c) {
+        bulk_g2s(st + g.h_off + c * RHZ + erow0 * Z,
+                 a.fin + (3 + c) * N + base + (long long)ey_lo * Z, hb, &full[slot]);
+        bulk_g2s(st + g.c_off + c * TYZ, a.cb + c * N + base + (long long)y0 * Z,
+                 cbb, &full[slot]);
+        bulk_g2s(st + g.m_off + c * g.MT,
+                 sa.mask_ws + ((long long)xp * 3 + c) * sa.Yp + ma, mbb, &full[slot]);
+      }
+      if (Pp > 0)
+        for (int c = 0; c < 4; ++c)
+          bulk_g2s(st + g.p_off + c * RH * Pp + erow0 * Pp,
+                   a.psi_in + c * PXY + ((long long)xp * Y + ey_lo) * Pp, pb,
+                   &full[slot]);
+    };
+    int nfill = 0;  // planes issued so far (x0 + nfill is the next one)
+    while (nfill < S && x0 + nfill <= xlast) {
+      fill(x0 + nfill, nfill, x0 + nfill < xe);
+      ++nfill;
+    }
+    bool ok = true;
+    int slot = 0;        // ring slot of plane x
+    uint32_t round = 0;  // fills of that slot before plane x's
+    for (int x = x0; x < xe && ok; ++x) {
+      const int k = x - x0;
+      const int b = k & 1;
+      ok = mbar_wait_or_abort(&done[slot], round & 1, sa.status, &abort_flag,
+                              sa.wait_cycles);
+      if (!ok) break;
+      if (x >= xs) {
+        float* hcur = hn + (size_t)b * 3 * RHZ;
+        float* ecur = en + (size_t)b * 3 * TYZ;
+        float* pcur = pn + (size_t)b * 4 * TY * Pp;
+        const long long base = (long long)x * YZ + (long long)y0 * Z;
+        const uint32_t fb = (uint32_t)(nrows * Z * 4);
+        for (int c = 0; c < 3; ++c) {
+          bulk_s2g(a.fout + (3 + c) * N + base, hcur + c * RHZ + Z, fb);
+          bulk_s2g(a.fout + c * N + base, ecur + c * TYZ, fb);
+        }
+        if (Pp > 0) {
+          const uint32_t pb = (uint32_t)(nrows * Pp * 4);
+          const long long pbase = ((long long)x * Y + y0) * Pp;
+          for (int c = 0; c < 4; ++c)
+            bulk_s2g(a.psi_out + c * PXY + pbase, pcur + c * TY * Pp, pb);
+        }
+        bulk_commit();
+      }
+      if (x0 + nfill <= xlast) {
+        fill(x0 + nfill, slot, x0 + nfill < xe);
+        ++nfill;
+      }
+      bulk_wait_read_all();
+      mbar_arrive(&freeb[b]);
+      if (++slot == S) {
+        slot = 0;
+        ++round;
+      }
+    }
+    for (int j = max(0, nfill - S); j < nfill; ++j)
+      mbar_wait(&full[j % S], (uint32_t)(j / S) & 1, sa.status, sa.wait_cycles);
+    bulk_wait_all();
+    return;
+  }
+
+  // ---------------- compute warps ----------------
+  // Item of this thread: interior warps first, then PML warps; item i is
+  // (buffer row i / Qn, quad i % Qn of the warp kind's quads).
+  const int QI = (Z - a.plo - a.phi) >> 2;
+  const int QP = (a.plo + a.phi) >> 2;
+  const int nwi = (RH * QI + 31) >> 5;
+  const bool pml = (tid >> 5) >= nwi;  // warp-uniform
+  const int it = pml ? tid - (nwi << 5) : tid;
+  const int Qn = pml ? QP : QI;
+  const int rH = Qn > 0 ? it / Qn : RH;
+  const int qi = it - rH * Qn;
+  const int lq = a.plo >> 2;
+  const int q = pml ? (qi < lq ? qi : (Z >> 2) - QP + qi) : lq + qi;
+  const int z0 = 4 * q;
+  const int col = 4 * qi;  // z-PML state column of z0 (PML warps)
+  const bool doH = rH < RH && y0 - 1 + rH >= 0 && y0 - 1 + rH < Y;
+  const int yE = y0 + rH;
+  const bool doE = rH < TY && yE < Y;
+  const bool zhi = z0 + 4 < Z;  // a z + 1 neighbour inside the domain
+  const bool zlo = z0 > 0;      // a z - 1 neighbour inside the domain
+
+  float ike[4], ikh[4], be[4], ce[4], bh[4], ch[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const int z = min(z0 + k, Z - 1);  // idle lanes read a valid entry
+    ike[k] = a.zc[z];
+    ikh[k] = a.zc[3 * Z + z];
+    be[k] = pml ? a.zc[Z + z] : 0.f;
+    ce[k] = pml ? a.zc[2 * Z + z] : 0.f;
+    bh[k] = pml ? a.zc[4 * Z + z] : 0.f;
+    ch[k] = pml ? a.zc[5 * Z + z] : 0.f;
+  }
+  const float mdt = -a.dt;
+  // Source box rows and z range of this item (the plane test is separate).
+  const bool src_row = a.snc > 0 && yE >= a.sy0 && yE < a.sy0 + a.sny &&
+                       z0 + 4 > a.sz0 && z0 < a.sz0 + a.snz;
+  const long long sb = (long long)a.snx * a.sny * a.snz;
+
+  const int ieH = rH * Z + z0;        // H-phase row rH, E rows rH / rH + 1
+  const int ihE = (rH + 1) * Z + z0;  // E-phase buffer row rH + 1
+  const int icE = rH * Z + z0;        // coefficient / staging row rH
+  const int pH = rH * Pp + col;
+  const int pE = (rH + 1) * Pp + col;
+
+  int slot = 0, slot1 = S > 1 ? 1 : 0;  // ring slots of planes x and x+1
+  uint32_t round = 0, round1 = S > 1 ? 0 : 1;
+  for (int x = x0; x < xe; ++x) {
+    const int k = x - x0;
+    const int b = k & 1;
+    const bool has_x1 = x + 1 < X;
+    bool ok = true;
+    if (k == 0)
+      ok = mbar_wait_or_abort(&full[slot], round & 1, sa.status, &abort_flag,
+                              sa.wait_cycles);
+    if (ok && has_x1)
+      ok = mbar_wait_or_abort(&full[slot1], round1 & 1, sa.status, &abort_flag,
+                              sa.wait_cycles);
+    if (ok && k >= 2)
+      ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
+                              &abort_flag, sa.wait_cycles);
+
+    const float* st = sm + (size_t)slot * g.stage;
+    const float* Es = st + g.e_off;
+    const float* E1 = sm + (size_t)slot1 * g.stage + g.e_off;
+    const float* Hs = st + g.h_off;
+    const float* Cs = st + g.c_off;
+    const float* Ms = st + g.m_off + moff;
+    const float* Ps = st + g.p_off;
+    float* hcur = hn + (size_t)b * 3 * RHZ;
+    const float* hprev = hn + (size_t)(b ^ 1) * 3 * RHZ;
+    float* ecur = en + (size_t)b * 3 * TYZ;
+    float* pcur = pn + (size_t)b * 4 * TY * Pp;
+
+    // H^{n+1/2}(x) of the quad at buffer row rH (y = y0 - 1 + rH).
+    if (ok && doH) {
+      float ex[4], ey[4], ez[4], exy[4], ezy[4], e1y[4], e1z[4], ho[3][4];
+      unpack4(lds4(Es + ieH), ex);
+      unpack4(lds4(Es + REZ + ieH), ey);
+      unpack4(lds4(Es + 2 * REZ + ieH), ez);
+      unpack4(lds4(Es + ieH + Z), exy);
+      unpack4(lds4(Es + 2 * REZ + ieH + Z), ezy);
+      const float exz = zhi ? Es[ieH + 4] : 0.f;
+      const float eyz = zhi ? Es[REZ + ieH + 4] : 0.f;
+      if (has_x1) {
+        unpack4(lds4(E1 + REZ + ieH), e1y);
+        unpack4(lds4(E1 + 2 * REZ + ieH), e1z);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) e1y[j] = e1z[j] = 0.f;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) unpack4(lds4(Hs + c * RHZ + ieH), ho[c]);
+      float pa[4], pb[4];
+      if (pml) {
+        unpack4(lds4(Ps + pH), pa);
+        unpack4(lds4(Ps + RH * Pp + pH), pb);
+      }
+      float hx[4], hy[4], hz[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float ey1 = j < 3 ? ey[j + 1] : eyz;
+        const float ex1 = j < 3 ? ex[j + 1] : exz;
+        const float dEz_y = fsub(ezy[j], ez[j]), dEy_z = fsub(ey1, ey[j]);
+        const float dEx_z = fsub(ex1, ex[j]), dEz_x = fsub(e1z[j], ez[j]);
+        const float dEy_x = fsub(e1y[j], ey[j]), dEx_y = fsub(exy[j], ex[j]);
+        float zEy, zEx;
+        if (pml) {
+          const float na = ffma(ch[j], dEy_z, fmul(bh[j], pa[j]));
+          const float nb = ffma(ch[j], dEx_z, fmul(bh[j], pb[j]));
+          pa[j] = na;
+          pb[j] = nb;
+          zEy = ffma(dEy_z, ikh[j], na);
+          zEx = ffma(dEx_z, ikh[j], nb);
+        } else {
+          zEy = fmul(dEy_z, ikh[j]);
+          zEx = fmul(dEx_z, ikh[j]);
+        }
+        hx[j] = ffma(mdt, fsub(dEz_y, zEy), ho[0][j]);
+        hy[j] = ffma(mdt, fsub(zEx, dEz_x), ho[1][j]);
+        hz[j] = ffma(mdt, fsub(dEy_x, dEx_y), ho[2][j]);
+      }
+      sts4(hcur + ieH, hx);
+      sts4(hcur + RHZ + ieH, hy);
+      sts4(hcur + 2 * RHZ + ieH, hz);
+      if (pml && rH > 0) {
+        sts4(pcur + (rH - 1) * Pp + col, pa);
+        sts4(pcur + TY * Pp + (rH - 1) * Pp + col, pb);
+      }
+    }
+    compute_sync(ncomp);
+    if (abort_flag) break;
+
+    // E^{n+1}(x) of the quad at tile row rH (y = y0 + rH).
+    if (x >= xs && doE) {
+      float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4], eo[3][4], cb[3][4];
+      unpack4(lds4(hcur + ihE), hx);
+      unpack4(lds4(hcur + RHZ + ihE), hy);
+      unpack4(lds4(hcur + 2 * RHZ + ihE), hz);
+      unpack4(lds4(hcur + ihE - Z), hxm);
+      unpack4(lds4(hcur + 2 * RHZ + ihE - Z), hzm);
+      const float hxz = zlo ? hcur[ihE - 1] : 0.f;
+      const float hyz = zlo ? hcur[RHZ + ihE - 1] : 0.f;
+      unpack4(lds4(hprev + RHZ + ihE), hyp);
+      unpack4(lds4(hprev + 2 * RHZ + ihE), hzp);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        unpack4(lds4(Es + c * REZ + ihE), eo[c]);
+        unpack4(lds4(Cs + c * TYZ + icE), cb[c]);
+      }
+      const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
+      float pa[4], pb[4];
+      if (pml) {
+        unpack4(lds4(Ps + 2 * RH * Pp + pE), pa);
+        unpack4(lds4(Ps + 3 * RH * Pp + pE), pb);
+      }
+      const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
+      float enew[3][4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float hy0 = j > 0 ? hy[j - 1] : hyz;
+        const float hx0 = j > 0 ? hx[j - 1] : hxz;
+        const float dHz_y = fsub(hz[j], hzm[j]), dHy_z = fsub(hy[j], hy0);
+        const float dHx_z = fsub(hx[j], hx0), dHz_x = fsub(hz[j], hzp[j]);
+        const float dHy_x = fsub(hy[j], hyp[j]), dHx_y = fsub(hx[j], hxm[j]);
+        float zHy, zHx;
+        if (pml) {
+          const float na = ffma(ce[j], dHy_z, fmul(be[j], pa[j]));
+          const float nb = ffma(ce[j], dHx_z, fmul(be[j], pb[j]));
+          pa[j] = na;
+          pb[j] = nb;
+          zHy = ffma(dHy_z, ike[j], na);
+          zHx = ffma(dHx_z, ike[j], nb);
+        } else {
+          zHy = fmul(dHy_z, ike[j]);
+          zHx = fmul(dHx_z, ike[j]);
+        }
+        float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
+        if (src) {
+          const int z = z0 + j;
+          if (z >= a.sz0 && z < a.sz0 + a.snz) {
+            const long long si =
+                ((long long)(x - a.sx0) * a.sny + (yE - a.sy0)) * a.snz + (z - a.sz0);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              float jc = 0.f;
+              for (int w = 0; w < a.snc; ++w)
+                jc = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], jc);
+              cur[c] = fsub(cur[c], jc);
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float rr = ffma(-sig[c], eo[c][j], cur[c]);
+          enew[c][j] = ffma(cb[c][j], rr, eo[c][j]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) sts4(ecur + c * TYZ + icE, enew[c]);
+      if (pml) {
+        sts4(pcur + 2 * TY * Pp + rH * Pp + col, pa);
+        sts4(pcur + 3 * TY * Pp + rH * Pp + col, pb);
+      }
+    }
+    // Publish this plane's results to the producer and release its slot.
+    fence_async_smem();
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(&done[slot]);
+    // H(x-1) (hprev) is rewritten by the next plane's H phase.
+    compute_sync(ncomp);
+    slot = slot1;
+    round = round1;
+    if (++slot1 == S) {
+      slot1 = 0;
+      ++round1;
+    }
+  }
+}
+
+// (zz, tile_y) shapes of the lean kernel: the streamed kernel's tile heights
+// for these zz with 4 ring stages.
+#define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29)
+
+template <int ZC, int TYC>
+__global__ void __launch_bounds__(384, 1) yee_lean_kernel(const StreamArgs sa) {
+  extern __shared__ __align__(16) float sm[];
+  lean_tile<ZC, TYC>(sa, blockIdx.x, blockIdx.y, sm);
+}
+
+}  // namespace pjzfdtd

@@ -23,6 +23,7 @@
 #include "step_kernel.cuh"
 #include "stream_kernel.cuh"
 #include "stream2_kernel.cuh"
+#include "lean_kernel.cuh"
 #include "record_kernel.cuh"
 #include "kernel_table.cuh"
 
@@ -62,7 +63,7 @@ struct pjzfdtd_plan {
   std::vector<float> weights;  // [rows][ns]
   // Resolved launch geometry.
   int tile_y = 0, seg_x = 0, threads = 0, steps_per_pass = 1;
-  int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed
+  int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed, 3 lean streamed
   int stages = 0;   // streamed ring depth
   size_t smem = 0;  // dynamic shared memory per CTA
   // Two-step kernel (steps_per_pass == 2): CTA size, ring depths (ring A in
@@ -284,18 +285,64 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   return PJZFDTD_OK;
 }
 
+// Whether auto selection takes the lean kernel where it applies.
+constexpr bool kLeanAuto = false;
+
+// Lean streamed kernel (lean_kernel.cuh) on top of a resolved streamed
+// plan: a compile-time (zz, tile_y) shape, one step per launch, z-PML slab
+// widths that are multiples of 4 (PML quads are whole), the source read
+// from global memory.  `required`: fail when it does not apply, else keep
+// the streamed plan.
+int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
+  const pjzfdtd_problem& p = pl->p;
+  const int Z = p.zz, ty = pl->tile_y;
+  const bool shape = lean_kernel_ptr(Z, ty) != nullptr;
+  const bool ok = shape && pl->steps_per_pass == 1 && p.pml_lo % 4 == 0 &&
+                  p.pml_hi % 4 == 0 && (required || pl->src_ring == 0);
+  if (!ok) {
+    if (!required) return PJZFDTD_OK;
+    return fail(PJZFDTD_ERR_UNSUPPORTED,
+                "the lean kernel needs (zz, tile_y) in {(64, 14), (48, 19), "
+                "(32, 29)} (got (%d, %d)), one step per launch and z-PML widths "
+                "that are multiples of 4 (got %d, %d)",
+                Z, ty, p.pml_lo, p.pml_hi);
+  }
+  const int warps = lean_warps_interior(Z, ty, p.pml_lo, p.pml_hi) +
+                    lean_warps_pml(ty, p.pml_lo, p.pml_hi);
+  if (warps * 32 + 32 > kLeanThreads)
+    return required ? fail(PJZFDTD_ERR_UNSUPPORTED, "lean tile needs %d warps",
+                           warps)
+                    : PJZFDTD_OK;
+  pl->kernel = 3;
+  pl->threads = warps * 32 + 32;
+  pl->src_ring = pl->src_rows = 0;
+  pl->smem = StreamGeom(ty, Z, pl->P).bytes(pl->stages);
+  return PJZFDTD_OK;
+}
+
 // Resolves the CTA tile.  Register-marching kernel: (tile_y + 2) * zz
 // cells, one thread each, at most kMaxThreads threads.
 int32_t resolve_tile(pjzfdtd_plan* pl) {
   const int Z = pl->p.zz;
-  if (pl->p.kernel < 0 || pl->p.kernel > 2)
+  if (pl->p.kernel < 0 || pl->p.kernel > 3)
     return fail(PJZFDTD_ERR_INVALID, "unknown kernel %d", pl->p.kernel);
   const int zmax = 2 * (kStreamThreads - 32);
-  if (pl->p.kernel == 2 && (Z % 4 != 0 || Z > zmax))
+  if (pl->p.kernel >= 2 && (Z % 4 != 0 || Z > zmax))
     return fail(PJZFDTD_ERR_INVALID,
-                "the streamed kernel needs zz %% 4 == 0 and zz <= %d", zmax);
-  if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax))
-    return resolve_stream(pl);
+                "the streamed kernels need zz %% 4 == 0 and zz <= %d", zmax);
+  if (pl->p.kernel == 3) {
+    if (pl->p.steps_per_pass == 2)
+      return fail(PJZFDTD_ERR_UNSUPPORTED,
+                  "the lean kernel advances one step per launch");
+    int32_t rc = resolve_stream(pl);
+    if (rc) return rc;
+    return resolve_lean(pl, true);
+  }
+  if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax)) {
+    int32_t rc = resolve_stream(pl);
+    if (rc || pl->p.kernel == 2 || !kLeanAuto) return rc;
+    return resolve_lean(pl, false);
+  }
   pl->kernel = 1;
   if (pl->p.steps_per_pass == 2)
     return fail(PJZFDTD_ERR_UNSUPPORTED,
@@ -365,7 +412,7 @@ void layout(pjzfdtd_plan* pl) {
   pl->off_comp = take(std::max<size_t>(comp, 1) * sizeof(float));
   pl->off_comph = take(std::max<size_t>(p.record_h ? comp : 0, 1) * sizeof(float));
   pl->off_status = take(sizeof(int));
-  pl->off_mask = take((pl->kernel == 2 ? (size_t)p.xx * 3 * pl->Yp : 1) * sizeof(float));
+  pl->off_mask = take((pl->kernel >= 2 ? (size_t)p.xx * 3 * pl->Yp : 1) * sizeof(float));
   pl->off_srcws = take((pl->src_ring > 0 ? (size_t)p.src_ncols * 3 * p.src_nx *
                                                p.src_ny * p.src_nz
                                          : 1) * sizeof(float));
@@ -381,6 +428,12 @@ StreamKernel stream_kernel_for(const pjzfdtd_plan* pl, bool sr) {
 
 cudaError_t set_stream_smem(const pjzfdtd_plan* pl, bool sr) {
   return cudaFuncSetAttribute(stream_kernel_for(pl, sr),
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)pl->smem);
+}
+
+cudaError_t set_lean_smem(const pjzfdtd_plan* pl) {
+  return cudaFuncSetAttribute(lean_kernel_ptr(pl->p.zz, pl->tile_y),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)pl->smem);
 }
@@ -410,6 +463,10 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
     CUDA_TRY(set_stream2_smem(pl));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, stream2_kernel_for(pl), pl->threads2, pl->smem2));
+  } else if (pl->kernel == 3) {
+    CUDA_TRY(set_lean_smem(pl));
+    CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, lean_kernel_ptr(pl->p.zz, pl->tile_y), pl->threads, pl->smem));
   } else if (pl->kernel == 2) {
     CUDA_TRY(set_stream_smem(pl, pl->src_ring > 0));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -522,7 +579,7 @@ int32_t run_init(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
       b->epsilon, b->absorption_mask, w.cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
       p.rx, p.ry, p.rz, p.dt);
   CUDA_TRY(cudaGetLastError());
-  if (pl->kernel == 2) {
+  if (pl->kernel >= 2) {
     const long long nm = (long long)p.xx * 3 * pl->Yp;
     pad_mask_kernel<<<(int)std::min<long long>((nm + 255) / 256, 1 << 16), 256, 0,
                       st>>>(b->absorption_mask, w.mask_ws, p.xx, p.yy, pl->Yp);
@@ -688,7 +745,10 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   const dim3 grid((p.yy + pl->tile_y - 1) / pl->tile_y,
                   (p.xx + pl->seg_x - 1) / pl->seg_x);
   StreamKernel sk = nullptr, sk2 = nullptr;
-  if (pl->kernel == 2) {
+  if (pl->kernel == 3) {
+    CUDA_TRY(set_lean_smem(pl));
+    sk = lean_kernel_ptr(p.zz, pl->tile_y);
+  } else if (pl->kernel == 2) {
     // Ring-carried source rows need an aligned source profile (fixed per run).
     const bool sr = stream_args(pl, ws, step_args(pl, b, ws, n0, pl->cur)).src_tma;
     CUDA_TRY(set_stream_smem(pl, sr));
@@ -702,7 +762,7 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
     const StepArgs a = step_args(pl, b, ws, ln.first, pl->cur);
     if (ln.second == 2) {
       sk2<<<grid, pl->threads2, pl->smem2, st>>>(stream_args(pl, ws, a));
-    } else if (pl->kernel == 2) {
+    } else if (pl->kernel >= 2) {
       sk<<<grid, pl->threads, pl->smem, st>>>(stream_args(pl, ws, a));
     } else {
       yee_step_kernel<<<grid, pl->threads, pl->smem, st>>>(a);
@@ -972,7 +1032,7 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
   size_t o = 0;
   for (int i = 0; i < n; ++i) {
     pjzfdtd_plan* pl = plans[i];
-    if (!pl || pl->kernel != 2) {
+    if (!pl || pl->kernel < 2) {
       delete bt;
       return fail(PJZFDTD_ERR_UNSUPPORTED,
                   "plan %d is not a streamed-kernel plan (zz %% 4 == 0 needed)", i);
@@ -1195,6 +1255,36 @@ void* g_static_ptr[kMaxDevices] = {};
 
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
+namespace {
+
+// Device address of the current device's scratch array.  The host cannot use
+// the array's symbol as a device address, so it is looked up with the device
+// current: on every call made outside a stream capture (so an address made
+// stale by cudaDeviceReset is replaced), and taken from the per-device cache
+// during a capture, which therefore needs one earlier call on that device.
+int32_t static_scratch(cudaStream_t st, void** out) {
+  int dev = 0;
+  CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices)
+    return fail(PJZFDTD_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+  std::lock_guard<std::mutex> lock(g_static_mu);
+  if (cap == cudaStreamCaptureStatusNone) {
+    void* p = nullptr;
+    CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
+    g_static_ptr[dev] = p;
+  } else if (!g_static_ptr[dev]) {
+    return fail(PJZFDTD_ERR_INVALID,
+                "the first static-scratch call on device %d was made during a "
+                "stream capture; make one call before capturing", dev);
+  }
+  *out = g_static_ptr[dev];
+  return PJZFDTD_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int32_t pjzfdtd_forward_static(pjzfdtd_plan* plan,
@@ -1208,24 +1298,24 @@ int32_t pjzfdtd_forward_static(pjzfdtd_plan* plan,
                 "has a fixed %zu-byte (64 MiB) array -- use pjzfdtd_forward "
                 "with a caller-allocated workspace",
                 plan->bytes, kStaticScratchBytes);
-  int dev = 0;
-  CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices)
-    return fail(PJZFDTD_ERR_UNSUPPORTED, "device %d beyond %d", dev, kMaxDevices);
+  const cudaStream_t st = static_cast<cudaStream_t>(stream);
   void* scratch = nullptr;
-  {
-    // Once per device, with that device current: the host cannot use the
-    // array's symbol as a device address, so resolve the real one.
-    std::lock_guard<std::mutex> lock(g_static_mu);
-    if (!g_static_ptr[dev]) {
-      void* p = nullptr;
-      CUDA_TRY(cudaGetSymbolAddress(&p, g_static_scratch));
-      g_static_ptr[dev] = p;
-    }
-    scratch = g_static_ptr[dev];
-  }
-  return run_range(plan, buffers, scratch, kStaticScratchBytes, 0, plan->p.tt,
-                   static_cast<cudaStream_t>(stream));
+  int32_t rc = static_scratch(st, &scratch);
+  if (rc) return rc;
+  return run_range(plan, buffers, scratch, kStaticScratchBytes, 0, plan->p.tt, st);
+}
+
+int32_t pjzfdtd_forward_static_status(pjzfdtd_plan* plan, void* stream) {
+  if (!plan) return fail(PJZFDTD_ERR_INVALID, "NULL plan");
+  if (plan->bytes > kStaticScratchBytes)
+    return fail(PJZFDTD_ERR_WORKSPACE,
+                "this plan needs %zu bytes of scratch, more than the %zu-byte "
+                "static array; it never ran through pjzfdtd_forward_static",
+                plan->bytes, kStaticScratchBytes);
+  void* scratch = nullptr;
+  int32_t rc = static_scratch(static_cast<cudaStream_t>(stream), &scratch);
+  if (rc) return rc;
+  return pjzfdtd_plan_status(plan, scratch, kStaticScratchBytes, stream);
 }
 
 }  // extern "C"

@@ -24,8 +24,12 @@
 // A z cell that lies wholly inside one layer (its fraction exactly 1, all
 // others exactly 0) has the same value at every such z of a column: it is
 // computed once per (y, layer) and copied, and only the cells an interface
-// cuts take the full mix.  Both give the same floats (the full mix adds
-// exact zeros to that layer's terms).  FP32 throughout; the per-cell
+// cuts take the full mix.  Both give the same floats when every layer's
+// window statistics at that (x, y) are finite (the full mix then adds exact
+// zeros to that layer's terms); where one is not (a zero pixel makes the
+// mean of the inverse infinite, a NaN pixel makes everything NaN), 0 * inf
+// in the full mix gives NaN as pjz's einsum does, so such columns take the
+// full mix at every z.  FP32 throughout; the per-cell
 // functions are __host__ __device__ so that a host emulation of the block
 // loop checks the same code on the CPU.
 #pragma once
@@ -74,9 +78,15 @@ PJZ_HD int render_imax(int a, int b) { return a > b ? a : b; }
 
 // Shared-memory floats of one CTA: occupancy [2][ll][zz], the layer that
 // fills each z cell [zz] (int, -1 when an interface cuts it), statistics
-// [kRenderTileY][ll] of 4 floats, one-layer values [kRenderTileY][ll].
+// [kRenderTileY][ll] of 4 floats, one-layer values [kRenderTileY][ll], and
+// per y cell whether every layer's statistics are finite [kRenderTileY]
+// (int).
 PJZ_HD size_t render_smem_floats(int ll, int zz) {
-  return 2 * (size_t)ll * zz + zz + 5 * (size_t)kRenderTileY * ll;
+  return 2 * (size_t)ll * zz + zz + 5 * (size_t)kRenderTileY * ll + kRenderTileY;
+}
+
+PJZ_HD bool render_finite(const WindowStats& w) {
+  return isfinite(w.mean) && isfinite(w.inv) && isfinite(w.gx) && isfinite(w.gy);
 }
 
 // Filled fraction of z cell `z` of component `c` by layer `l`, and the
@@ -178,19 +188,23 @@ __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a)
   int* owner = reinterpret_cast<int*>(mid + a.ll * a.zz);
   WindowStats* st = reinterpret_cast<WindowStats*>(owner + a.zz);
   float* ival = reinterpret_cast<float*>(st + kRenderTileY * a.ll);
+  int* yfin = reinterpret_cast<int*>(ival + kRenderTileY * a.ll);
   for (int z = threadIdx.x; z < a.zz; z += blockDim.x) {
     for (int l = 0; l < a.ll; ++l)
       render_occupancy(a, c, l, z, &frac[l * a.zz + z], &mid[l * a.zz + z]);
     owner[z] = render_owner(a, frac, z);
   }
+  if (threadIdx.x < kRenderTileY) yfin[threadIdx.x] = 1;
+  __syncthreads();
   for (int i = threadIdx.x; i < ny * a.ll; i += blockDim.x) {
     st[i] = render_window(a, c, i % a.ll, x, y0 + i / a.ll);
     ival[i] = render_interior(a, c, st[i]);
+    if (!render_finite(st[i])) yfin[i / a.ll] = 0;  // every writer stores 0
   }
   __syncthreads();
   for (int i = threadIdx.x; i < ny * a.zz; i += blockDim.x) {
     const int yl = i / a.zz, z = i - yl * a.zz;
-    const int o = owner[z];
+    const int o = yfin[yl] ? owner[z] : -1;
     a.out[render_out_index(a, c, x, y0 + yl, z)] =
         o >= 0 ? ival[yl * a.ll + o] : render_value(a, c, st + yl * a.ll, frac, mid, z);
   }

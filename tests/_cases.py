@@ -39,3 +39,28 @@ def random_problem(seed, X=24, Y=20, Z=16, tt=48, pml=(2, 2), src="x",
 def oracle_kwargs(case):
   return {k: v for k, v in case.items()
           if k not in ("source_field", "source_position", "domain")}
+
+
+def field_oracle(wl, precision="f32", nthreads=0):
+  """pjz's ``field`` of workload ``wl`` on the CPU oracle: the restated
+  pre-processing (``oracle/pjz_ref.py``), the C Yee update in FP32 or FP64
+  and the pinv projection accumulated at the sample steps; returns the
+  complex ``(ww, 3, xx, yy, zz)`` fields."""
+  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
+                                  pjz_ref.SimParams(*wl.sim_params[:-1]),
+                                  zz=wl.domain[2])
+  domain = (kw["absorption_mask"].shape[1], kw["absorption_mask"].shape[2],
+            kw["pml_kappa"].shape[0])
+  org, shp, prof = oracle.plane_source_box(kw["source_field"],
+                                           kw["source_position"], domain)
+  w = pjz_ref.projection_weights(omega, kw["output_steps"], kw["dt"])
+  r = oracle.run(eps=kw["epsilon"], offset=kw["offset"],
+                 mask=kw["absorption_mask"], kappa=kw["pml_kappa"],
+                 sigma=kw["pml_sigma"], alpha=kw["pml_alpha"], dt=kw["dt"],
+                 tt=kw["source_waveform"].shape[0], pml_widths=kw["pml_widths"],
+                 source_origin=org, source_profile=prof,
+                 waveform=kw["source_waveform"], output_steps=kw["output_steps"],
+                 mode="project", weights=w, precision=precision,
+                 nthreads=nthreads)["out"]
+  ww = omega.shape[0]
+  return r[:ww] + 1j * r[ww:]

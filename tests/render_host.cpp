@@ -41,7 +41,9 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   int* owner = reinterpret_cast<int*>(mid + ll * zz);
   WindowStats* st = reinterpret_cast<WindowStats*>(owner + zz);
   float* ival = reinterpret_cast<float*>(st + kRenderTileY * ll);
-  if (ival + kRenderTileY * ll != sm.data() + sm.size()) return 1;  // carving
+  int* yfin = reinterpret_cast<int*>(ival + kRenderTileY * ll);
+  if (reinterpret_cast<float*>(yfin + kRenderTileY) != sm.data() + sm.size())
+    return 1;  // carving
   for (int c = 0; c < 3; ++c)
     for (int x = 0; x < xx; ++x)
       for (int y0 = 0; y0 < yy; y0 += kRenderTileY) {
@@ -51,9 +53,11 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
             render_occupancy(a, c, l, z, &frac[l * zz + z], &mid[l * zz + z]);
           owner[z] = render_owner(a, frac, z);
         }
+        for (int i = 0; i < kRenderTileY; ++i) yfin[i] = 1;
         for (int i = 0; i < ny * ll; ++i) {
           st[i] = render_window(a, c, i % ll, x, y0 + i / ll);
           ival[i] = render_interior(a, c, st[i]);
+          if (!render_finite(st[i])) yfin[i / ll] = 0;
         }
         for (int i = 0; i < ny * zz; ++i) {
           const int yl = i / zz, z = i - yl * zz;
@@ -62,7 +66,7 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
             g_render_bad = 1;
             continue;
           }
-          const int w = owner[z];
+          const int w = yfin[yl] ? owner[z] : -1;
           out[o] = w >= 0 ? ival[yl * ll + w]
                           : render_value(a, c, st + yl * ll, frac, mid, z);
         }

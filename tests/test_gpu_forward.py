@@ -14,7 +14,7 @@ import oracle
 from oracle import pjz_ref
 from pjz_gb300 import engine, workloads
 import pjz_gb300
-from _cases import oracle_kwargs, random_problem
+from _cases import field_oracle, oracle_kwargs, random_problem
 
 pytestmark = pytest.mark.gpu
 DEV = torch.device("cuda:0")
@@ -205,24 +205,7 @@ def test_fdtdz_dropin_matches_oracle(native):
   assert np.array_equal(out.cpu().numpy(), want)
 
 
-def _field_oracle(wl, precision="f32"):
-  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
-                                  pjz_ref.SimParams(*wl.sim_params[:-1]),
-                                  zz=wl.domain[2])
-  domain = (kw["absorption_mask"].shape[1], kw["absorption_mask"].shape[2],
-            kw["pml_kappa"].shape[0])
-  org, shp, prof = oracle.plane_source_box(kw["source_field"],
-                                           kw["source_position"], domain)
-  w = pjz_ref.projection_weights(omega, kw["output_steps"], kw["dt"])
-  r = oracle.run(eps=kw["epsilon"], offset=kw["offset"],
-                 mask=kw["absorption_mask"], kappa=kw["pml_kappa"],
-                 sigma=kw["pml_sigma"], alpha=kw["pml_alpha"], dt=kw["dt"],
-                 tt=kw["source_waveform"].shape[0], pml_widths=kw["pml_widths"],
-                 source_origin=org, source_profile=prof,
-                 waveform=kw["source_waveform"], output_steps=kw["output_steps"],
-                 mode="project", weights=w, precision=precision)["out"]
-  ww = omega.shape[0]
-  return r[:ww] + 1j * r[ww:]
+_field_oracle = field_oracle
 
 
 def test_field_short_c0_bit_exact(native):

@@ -3,7 +3,7 @@ render kernel): against the FP64 oracle on uneven shapes (relative 2e-5,
 FP32 against FP64), against every expected value of pjz's layer tests, and
 against the host emulation of the same kernel code on a production-size
 stack (512 x 512 cells at 2x magnification, 3 layers, zz 64; relative
-1e-6).  The file sorts last so that the solver's GPU tests run first."""
+1e-6), and the NaN pattern of a stack with a zero or NaN pixel."""
 
 import numpy as np
 import pytest
@@ -91,3 +91,24 @@ def test_gpu_matches_host_emulation_production_size(native, host):
   print(f"render 512x512x64 (3 layers, 2x): {e0.elapsed_time(e1):.3f} ms")
   np.testing.assert_allclose(out.cpu().numpy(), render(host, layers, pos, m, zz),
                              rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("bad", [0.0, np.nan])
+@pytest.mark.parametrize("simple", [False, True])
+def test_gpu_nonfinite_window_matches_oracle_pattern(native, bad, simple):
+  """A zero pixel (infinite inverse) or a NaN pixel in one layer gives the
+  NaN / inf pattern of pjz's einsum (0 * inf = NaN) in every z cell of that
+  column, including cells another layer fills."""
+  rng = np.random.default_rng(3)
+  m, zz = 1, 8
+  layers = rng.uniform(2.0, 12.0, (3, 2 * m * 5, 2 * m * 6)).astype(np.float32)
+  layers[0, 4, 5] = bad
+  pos = np.array([2.5, 5.0], np.float32)
+  with np.errstate(divide="ignore", invalid="ignore"):
+    want = eo.epsilon(layers.astype(np.float64), pos.astype(np.float64), m, zz,
+                      simple)
+  got = _gpu(layers, pos, m, zz, simple)
+  np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+  np.testing.assert_array_equal(np.isinf(got), np.isinf(want))
+  ok = np.isfinite(want)
+  np.testing.assert_allclose(got[ok], want[ok], rtol=2e-5, atol=0)

@@ -37,7 +37,7 @@ def host(tmp_path_factory):
   return h
 
 
-def render(host, layers, pos, m, zz, simple=False):
+def render(host, layers, pos, m, zz, simple=False, finite=True):
   layers = np.ascontiguousarray(layers, np.float32)
   ll, px, py = layers.shape
   xx, yy = px // (2 * m), py // (2 * m)
@@ -47,7 +47,8 @@ def render(host, layers, pos, m, zz, simple=False):
                          pos.ctypes.data if pos.size else None, int(simple),
                          out.ctypes.data)
   assert bad == 0, "a read or write left its array"
-  assert np.isfinite(out).all(), "an output was not written"
+  if finite:
+    assert np.isfinite(out).all(), "an output was not written"
   return out
 
 
@@ -106,6 +107,31 @@ def test_reference_layer_tables(host):
         pytest.approx(c["expected"], rel=1e-5)
     n += 1
   assert n == 93
+
+
+@pytest.mark.parametrize("bad", [0.0, np.nan, np.inf])
+@pytest.mark.parametrize("simple", [False, True])
+def test_nonfinite_window_gives_the_oracle_nan_pattern(host, bad, simple):
+  """A zero, NaN or infinite pixel in one layer: pjz's einsum multiplies
+  that layer's statistics by the zero fractions of the cells other layers
+  fill (0 * inf = NaN), so the whole column follows; the one-layer
+  shortcut must not hide it."""
+  rng = np.random.default_rng(3)
+  m, zz = 1, 8
+  layers = rng.uniform(2.0, 12.0, (3, 2 * m * 5, 2 * m * 6)).astype(np.float32)
+  layers[0, 4, 5] = bad
+  pos = np.array([2.5, 5.0], np.float32)
+  with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+    want = eo.epsilon(layers.astype(np.float64), pos.astype(np.float64), m, zz,
+                      simple)
+  got = render(host, layers, pos, m, zz, simple, finite=False)
+  # With simple averaging only the mean enters, which a zero pixel keeps
+  # finite.
+  assert np.isfinite(want).all() == (simple and bad == 0.0)
+  np.testing.assert_array_equal(np.isnan(got), np.isnan(want))
+  np.testing.assert_array_equal(np.isinf(got), np.isinf(want))
+  ok = np.isfinite(want)
+  np.testing.assert_allclose(got[ok], want[ok], rtol=2e-5, atol=0)
 
 
 @pytest.mark.parametrize("shape,pos,m,msg", [

@@ -30,6 +30,12 @@ before it is made in the kernel.
 It mirrors the kernels' index arithmetic line for line (the shared helpers
 `h_pair` / `e_pair` follow the kernels' helpers of the same names); a
 kernel change to that arithmetic must change this model with it.
+
+The lean one-step kernel (`csrc/lean_kernel.cuh`) shares the streamed
+kernel's layout and producer, so its replay is the one-step replay with the
+compute accesses swapped for the lean ones (`lean_items`, `lean_h`,
+`lean_e`): one z-quad per thread, 128-bit accesses (checked 16-byte
+aligned), interior and z-PML quads on separate warps.
 """
 
 import itertools
@@ -81,6 +87,8 @@ class Smem:
       off = np.clip(off, 0, len(self.tag) - width)
     if width == 2 and np.any(off % 2):
       self.bad.append((what, "align8", int(off[off % 2 != 0][0])))
+    if width == 4 and np.any(off % 4):
+      self.bad.append((what, "align16", int(off[off % 4 != 0][0])))
     return off
 
   def read(self, what, off, thr, expect, zero_ok, lo, hi, width=1):
@@ -232,8 +240,121 @@ def pml_columns(Z, plo, phi):
   return z0s, pz
 
 
+def lean_items(Z, TY, plo, phi):
+  """Every compute thread's item in the lean kernel: thread ids, buffer row
+  rH, quad start z0, z-PML state column and whether the thread is on a PML
+  warp -- interior warps first (quads plo/4 .. (Z-phi)/4 - 1 of each row),
+  then PML warps (the slab quads, state column 4 * index)."""
+  RH = TY + 1
+  QI, QP = (Z - plo - phi) // 4, (plo + phi) // 4
+  lq = plo // 4
+  nwi = (RH * QI + 31) // 32
+  nwp = (RH * QP + 31) // 32
+  it = np.arange(32 * nwi)
+  thr_i, rH_i = it, it // QI
+  z0_i = 4 * (lq + it % QI)
+  if QP:
+    ip = np.arange(32 * nwp)
+    qi = ip % QP
+    thr_p, rH_p = 32 * nwi + ip, ip // QP
+    z0_p = 4 * np.where(qi < lq, qi, Z // 4 - QP + qi)
+    col_p = 4 * qi
+  else:
+    thr_p = rH_p = z0_p = col_p = np.zeros(0, np.int64)
+  thr = np.concatenate([thr_i, thr_p])
+  rH = np.concatenate([rH_i, rH_p])
+  z0 = np.concatenate([z0_i, z0_p])
+  col = np.concatenate([np.zeros_like(thr_i), col_p])
+  pml = np.concatenate([np.zeros(len(thr_i), bool), np.ones(len(thr_p), bool)])
+  return thr, rH, z0, col, pml, 32 * (nwi + nwp)
+
+
+def lean_h(sm, it, Z, Y, Pp, y0, RH, ieH, ring_e, ring_e1, ring_h, ring_p,
+           hcur, RHZ, pcur, po_hi, TY, x):
+  """H-phase accesses of the lean kernel's items `it` (a boolean selection
+  of lean_items) at plane x."""
+  thr, rH, z0, col, pml = it
+  y = y0 - 1 + rH
+  ie = ieH
+  Ep = ring_e
+  for c in range(3):
+    sm.read("LH:E", Ep.base + c * Ep.stride + ie, thr, Ep.T(c, y), False, Ep.lo,
+            Ep.hi, 4)
+  up = y + 1 >= Y
+  sm.read("LH:Ex y+1", Ep.base + ie + Z, thr, Ep.T(0, y + 1), up, Ep.lo, Ep.hi, 4)
+  sm.read("LH:Ez y+1", Ep.base + 2 * Ep.stride + ie + Z, thr, Ep.T(2, y + 1), up,
+          Ep.lo, Ep.hi, 4)
+  zin = z0 + 4 < Z
+  sm.read("LH:Ex z+1", (Ep.base + ie + 4)[zin], thr[zin], Ep.T(0, y[zin]), False,
+          Ep.lo, Ep.hi)
+  sm.read("LH:Ey z+1", (Ep.base + Ep.stride + ie + 4)[zin], thr[zin],
+          Ep.T(1, y[zin]), False, Ep.lo, Ep.hi)
+  if ring_e1 is not None:
+    for c in (1, 2):
+      sm.read("LH:E x+1", ring_e1.base + c * ring_e1.stride + ie, thr,
+              ring_e1.T(c, y), False, ring_e1.lo, ring_e1.hi, 4)
+  for c in range(3):
+    sm.read("LH:H", ring_h.base + c * ring_h.stride + ie, thr, ring_h.T(c, y), False,
+            ring_h.lo, ring_h.hi, 4)
+  pi = rH * Pp + col
+  for c in range(2):
+    sm.read("LH:psi", (ring_p.base + c * ring_p.stride + pi)[pml], thr[pml],
+            ring_p.T(c, y[pml]), False, ring_p.lo, ring_p.hi, 4)
+  for c in range(3):
+    sm.write("LH out", hcur + c * RHZ + ie, thr, tag(H + c, 1, x, y), hcur,
+             hcur + 3 * RHZ, 4)
+  sel = pml & (rH > 0)
+  po = (rH - 1) * Pp + col
+  for c in range(2):
+    sm.write("LH:psi out", (pcur + c * TY * Pp + po)[sel], thr[sel],
+             tag(PSI + c, 1, x, y[sel]), pcur, po_hi, 4)
+
+
+def lean_e(sm, it, Z, Pp, y0, RH, TY, hcur, hprev, RHZ, x, ring_e, Cs, c_lo, Ms,
+           m_lo, MT, m_n, ring_p, ecur, pcur, po_hi):
+  """E-phase accesses of the lean kernel's items `it` at plane x."""
+  thr, rH, z0, col, pml = it
+  y = y0 + rH
+  ih = (rH + 1) * Z + z0
+  ic = rH * Z + z0
+  for c in range(3):
+    sm.read("LE:H", hcur + c * RHZ + ih, thr, tag(H + c, 1, x, y), False, hcur,
+            hcur + 3 * RHZ, 4)
+  down = y - 1 < 0
+  sm.read("LE:Hx y-1", hcur + ih - Z, thr, tag(H + 0, 1, x, y - 1), down, hcur,
+          hcur + 3 * RHZ, 4)
+  sm.read("LE:Hz y-1", hcur + 2 * RHZ + ih - Z, thr, tag(H + 2, 1, x, y - 1), down,
+          hcur, hcur + 3 * RHZ, 4)
+  zin = z0 > 0
+  sm.read("LE:Hx z-1", (hcur + ih - 1)[zin], thr[zin], tag(H + 0, 1, x, y[zin]),
+          False, hcur, hcur + 3 * RHZ)
+  sm.read("LE:Hy z-1", (hcur + RHZ + ih - 1)[zin], thr[zin], tag(H + 1, 1, x, y[zin]),
+          False, hcur, hcur + 3 * RHZ)
+  for c in (1, 2):
+    sm.read("LE:H x-1", hprev + c * RHZ + ih, thr, tag(H + c, 1, x - 1, y), x == 0,
+            hprev, hprev + 3 * RHZ, 4)
+  for c in range(3):
+    sm.read("LE:E", ring_e.base + c * ring_e.stride + ih, thr, ring_e.T(c, y), False,
+            ring_e.lo, ring_e.hi, 4)
+    sm.read("LE:cb", Cs + c * TY * Z + ic, thr, tag(CB + c, 0, x, y), False, c_lo,
+            c_lo + 3 * TY * Z, 4)
+    sm.read("LE:mask", Ms + c * MT + rH, thr, tag(MASK + c, 0, x, y), False,
+            m_lo + c * MT, m_lo + c * MT + m_n)
+  pi = (rH + 1) * Pp + col
+  for c in range(2):
+    sm.read("LE:psi", (ring_p.base + (2 + c) * ring_p.stride + pi)[pml], thr[pml],
+            ring_p.T(2 + c, y[pml]), False, ring_p.lo, ring_p.hi, 4)
+  for c in range(3):
+    sm.write("LE out", ecur + c * TY * Z + ic, thr, tag(E + c, 1, x, y), ecur,
+             ecur + 3 * TY * Z, 4)
+  po = rH * Pp + col
+  for c in (2, 3):
+    sm.write("LE:psi out", (pcur + c * TY * Pp + po)[pml], thr[pml],
+             tag(PSI + c, 1, x, y[pml]), pcur, po_hi, 4)
+
+
 def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
-                 plant=None, hbuf=2, barriers=2):
+                 plant=None, hbuf=2, barriers=2, lean=False):
   """Replays CTA (tile, seg) of yee_stream_kernel; returns its Smem or None
   when the host refuses the tile.  `cover[x, y]` counts the rows stored.
   `plant` puts a known mistake into the replay (for the tests that show the
@@ -262,7 +383,7 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   if smem_bytes(0) > SMEM_BUDGET:
     return None
   sw, sx0, sy0, sz0, snx, sny, snz, snc, srowf = 0, 0, 0, 0, 0, 0, 0, 0, 0
-  if src is not None:
+  if src is not None and not lean:
     sx0, sy0, sz0, snx, sny, snz, snc = src
     srowf = snc * 3 * snz
     rows = min(TY, sny)
@@ -279,6 +400,7 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
 
   Zh = Z // 2
   rpt = ncomp // Zh
+  litems = lean_items(Z, TY, plo, phi) if lean else None
   y0 = tile * TY
   xs = seg * seg_x
   xe = min(X, xs + seg_x)
@@ -351,7 +473,13 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
     # H phase: rows r = rt, rt + rpt, ... of threads rt < rpt.
     ras, ys, thr = phase_rows(0, RH, lambda r: y0 - 1 + r, lambda y: 0 <= y < Y, rpt,
                               Zh, z0s)
-    if len(ras):
+    if lean:
+      yH = y0 - 1 + litems[1]
+      sel = (litems[1] < RH) & (yH >= 0) & (yH < Y)
+      it = tuple(v[sel] for v in litems[:5])
+      lean_h(sm, it, Z, Y, Pp, y0, RH, it[1] * Z + it[2], ring_e, ring_e1, ring_h,
+             ring_p, hcur, RHZ, pcur, po_hi, TY, x)
+    elif len(ras):
       h_pair(sm, "H", thr, z0s, pz, Z, Y, Pp, ras, ys, ring_e, ring_e1, ring_h, ring_p)
       r, y = ras[:, None], ys[:, None]
       ie = r * Z + z0s
@@ -391,8 +519,16 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
       ring_pe = Ptr(Ps + 2 * RH * Pp, RH * Pp, Ps, Ps + 4 * RH * Pp,
                     lambda c, y, x=x: tag(PSI + 2 + c, 0, x, y))
       ras, ys, thr = phase_rows(0, TY, lambda r: y0 + r, lambda y: y < Y, rpt, Zh, z0s)
-      e_pair(sm, "E", thr, z0s, pz, Z, Pp, ras + 1, ys, hc[0], hc[1], hc[2], hp[1],
-             hp[2], x == 0, ring_e, ring_cb, ring_pe)
+      if lean:
+        sel = (litems[1] < TY) & (y0 + litems[1] < Y)
+        it = tuple(v[sel] for v in litems[:5])
+        lean_e(sm, it, Z, Pp, y0, RH, TY, hcur, hprev, RHZ, x, ring_e, Cs, Cs, Ms,
+               st + m_off, MT, mb - ma, ring_p, ecur, pcur, po_hi)
+        ras = ys = np.zeros(0, np.int64)
+        thr = np.zeros((0, len(z0s)), np.int64)
+      else:
+        e_pair(sm, "E", thr, z0s, pz, Z, Pp, ras + 1, ys, hc[0], hc[1], hc[2], hp[1],
+               hp[2], x == 0, ring_e, ring_cb, ring_pe)
       r, y = ras[:, None], ys[:, None]
       for c in range(3):
         sm.read("E:mask", Ms + c * MT + ras, thr[:, 0], tag(MASK + c, 0, x, ys), False,
@@ -645,10 +781,10 @@ def run_grid(cta, X, Y, TY, seg_x, cover_shape):
 
 
 def one_step(X, Y, Z, plo, phi, TY, S, seg_x, ncomp, src, plant=None, hbuf=2,
-             barriers=2):
+             barriers=2, lean=False):
   def cta(tile, seg, cover):
     return one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src,
-                        cover, plant, hbuf, barriers)
+                        cover, plant, hbuf, barriers, lean)
   return run_grid(cta, X, Y, TY, seg_x, (X, Y))
 
 
@@ -809,3 +945,55 @@ def test_random_shapes():
     if res is not None:
       assert not res[1] and (res[2] == 1).all(), (X, Y, Z, plo, phi, TY2, seg,
                                                    nc2, res[1][:2])
+
+
+LEAN_CASES = [(5, 30, 64, 14), (4, 41, 48, 19), (3, 61, 32, 29), (6, 9, 16, 5),
+              (4, 13, 24, 3)]
+
+
+@pytest.mark.parametrize("X,Y,Z,TY", LEAN_CASES)
+@pytest.mark.parametrize("plo,phi", [(0, 0), (4, 4), (8, 8), (4, 8), (12, 4)])
+def test_lean_compute_accesses(X, Y, Z, TY, plo, phi):
+  """The lean kernel's items (z-quads, interior and PML warps) over ring
+  depths and segments, with a tile boundary inside the domain and a ragged
+  last tile: in bounds, 16-byte aligned, reading exactly the data each
+  update needs, race-free between barriers, every row stored once."""
+  if plo + phi > Z:
+    pytest.skip("slabs wider than the domain")
+  checked = 0
+  for S, seg_x in itertools.product((2, 3, 4), (2, X)):
+    res = one_step(X, Y, Z, plo, phi, TY, S, seg_x, min_ncomp(Z), None, lean=True)
+    if res is None:
+      continue
+    reads, bad, cover = res
+    assert not bad, (X, Y, Z, TY, plo, phi, S, seg_x, bad[:3])
+    assert (cover == 1).all(), (S, seg_x)
+    checked += reads
+  assert checked > 0
+
+
+def test_lean_items_cover_each_quad_once():
+  """Interior and PML warps together hold every (row, quad) of the H phase
+  exactly once, PML items only z-PML quads, and the PML state column of a
+  PML quad is its z-PML column."""
+  for Z, TY, plo, phi in [(64, 14, 8, 8), (48, 19, 4, 12), (32, 29, 0, 0),
+                          (64, 14, 12, 0)]:
+    thr, rH, z0, col, pml, n = lean_items(Z, TY, plo, phi)
+    assert n % 32 == 0 and len(np.unique(thr)) == len(thr)
+    live = rH < TY + 1
+    pairs = set(zip(rH[live].tolist(), z0[live].tolist()))
+    assert len(pairs) == live.sum() == (TY + 1) * Z // 4
+    zp = z0[live & pml]
+    assert ((zp < plo) | (zp >= Z - phi)).all()
+    zc = np.where(zp < plo, zp, zp - (Z - phi) + plo)
+    assert (zc == col[live & pml]).all()
+    # whole warps of one kind
+    assert len(np.unique(pml.reshape(-1, 32), axis=1)[0]) <= 2
+
+
+def test_lean_model_flags_a_planted_mistake():
+  """A lean replay whose absorber offset is dropped reads stale data."""
+  args = (5, 30, 64, 8, 8, 14, 3, 2, 32, None)
+  assert one_step(*args, lean=True)[1] == []
+  res = one_step(*args, plant="moff", lean=True)
+  assert any(b[2] == "LE:mask" and b[3] == "stale" for b in res[1])
