@@ -220,7 +220,8 @@ def torch_eager_baseline(kw, org, prof, domain, wl, seconds, threads):
 
   t1 = run(1)
   per = max(run(3) - t1, 1e-6) / 2
-  n = max(2, min(wl.sim_params.tt, int(seconds / per)))
+  # 1 + n steps must fit the waveform's tt rows.
+  n = max(2, min(wl.sim_params.tt - 1, int(seconds / per)))
   dt = run(1 + n) - t1
   cells = np.prod(domain) * n
   return {"value": cells / max(dt, 1e-9) / 1e9, "unit": UNIT, "cores": threads,

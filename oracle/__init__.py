@@ -62,7 +62,7 @@ class Problem(ctypes.Structure):
       (n, ctypes.c_int32) for n in (
           "sx0", "sy0", "sz0", "snx", "sny", "snz", "snc",
           "out_start", "out_stop", "out_step", "mode", "nrows", "record_h",
-          "gx0", "gy0", "gz0", "gnx", "gny", "gnz", "nthreads")]
+          "gx0", "gy0", "gz0", "gnx", "gny", "gnz", "nthreads", "storage")]
 
 
 _lib = None
@@ -77,6 +77,8 @@ def _load():
       fn = getattr(_lib, name)
       fn.restype = ctypes.c_int
       fn.argtypes = [ctypes.POINTER(Problem)] + [ctypes.c_void_p] * 12
+    _lib.oracle_round_f16.restype = ctypes.c_float
+    _lib.oracle_round_f16.argtypes = [ctypes.c_float]
   return _lib
 
 
@@ -124,7 +126,8 @@ def plane_source_box(source_field, source_position, domain):
 def run(*, eps, offset, mask, kappa, sigma, alpha, dt, tt, pml_widths,
         source_origin, source_profile, waveform, output_steps=(0, 0, 1),
         mode="snapshot", weights=None, q=None, grad_origin=(0, 0, 0),
-        record_h=False, fields=None, precision="f32", nthreads=0):
+        record_h=False, fields=None, precision="f32", nthreads=0,
+        storage="f32"):
   """Runs ``tt`` Yee steps on the CPU; returns a dict of outputs.
 
   ``eps`` (3,rx,ry,rz) at ``offset``; ``mask`` (3,X,Y) defines X, Y;
@@ -134,7 +137,9 @@ def run(*, eps, offset, mask, kappa, sigma, alpha, dt, tt, pml_widths,
   as ``(ns, 3, rx, ry, rz)``; ``project`` returns ``weights @ snapshots``
   (rows x 3 x region) with compensated FP summation; ``grad`` returns the
   per-cell sum over samples of ``E * (weights[:, j] . q)`` over the box
-  ``q.shape[2:]`` at ``grad_origin``.
+  ``q.shape[2:]`` at ``grad_origin``.  ``storage="f16"`` (with
+  ``precision="f32"``) rounds every stored field, CPML state and E-update
+  coefficient to binary16, the engine's reduced-precision storage.
   """
   lib = _load()
   real = np.float32 if precision == "f32" else np.float64
@@ -160,6 +165,9 @@ def run(*, eps, offset, mask, kappa, sigma, alpha, dt, tt, pml_widths,
   p.mode = MODES[mode]
   p.record_h = int(record_h)
   p.nthreads = nthreads
+  if storage not in ("f32", "f16") or (storage == "f16" and precision != "f32"):
+    raise ValueError("storage must be 'f32', or 'f16' with precision 'f32'")
+  p.storage = 1 if storage == "f16" else 0
   ns = len(range(*output_steps))
   R = (p.rx, p.ry, p.rz)
   out = out_h = None
@@ -190,3 +198,8 @@ def run(*, eps, offset, mask, kappa, sigma, alpha, dt, tt, pml_widths,
   if rc != 0:
     raise ValueError(f"oracle rejected the problem (code {rc})")
   return {"out": out, "out_h": out_h, "fields": fields}
+
+
+def round_f16(v: float) -> float:
+  """The oracle's binary16 rounding of one float (round to nearest even)."""
+  return float(_load().oracle_round_f16(float(v)))

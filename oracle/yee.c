@@ -32,6 +32,13 @@
  * fixed order, built with -ffp-contract=off) so that the FP32 build performs
  * the same IEEE operations as the CUDA kernels; the FP64 build (REAL=double)
  * is the higher-precision reference the FP32 error is stated against.
+ *
+ * Reduced-precision storage (storage = 1, FP32 build only) restates pjz's
+ * use_reduced_precision (src/pjz/_field.py:52) as 16-bit IEEE storage with
+ * FP32 arithmetic: every stored E, H and CPML state value and the E-update
+ * coefficient cb are rounded to binary16 (round to nearest even) when
+ * written; reads widen them exactly; the update in between, the source sums
+ * and the phasor accumulators stay FP32.
  */
 #include <math.h>
 #include <stdint.h>
@@ -47,10 +54,13 @@
 #define SUFFIX(name) name##_f32
 /* FP32: coefficients are rounded to float exactly as the engine does. */
 #define COEF(v) ((REAL)(float)(v))
+#define STORE(v) (half ? (REAL)round_f16((float)(v)) : (v))
+#define ORACLE_F32 1
 #else
 #define FMA fma
 #define SUFFIX(name) name##_f64
 #define COEF(v) ((REAL)(v))
+#define STORE(v) (v)
 #endif
 
 typedef struct {
@@ -68,7 +78,15 @@ typedef struct {
   int32_t record_h;            /* also record H (modes 1 and 2) */
   int32_t gx0, gy0, gz0, gnx, gny, gnz; /* gradient box (mode 3) */
   int32_t nthreads;
+  int32_t storage;             /* 0 FP32, 1 binary16 (FP32 build only) */
 } oracle_problem;
+
+/* Rounds v to binary16 (round to nearest even, subnormals kept) and back. */
+static inline float round_f16(float v) { return (float)(_Float16)v; }
+
+#ifdef ORACLE_F32
+float oracle_round_f16(float v) { return round_f16(v); }
+#endif
 
 static void pml_coeff(double kappa, double sigma, double alpha, double dt,
                       double* ik, double* b, double* c) {
@@ -108,6 +126,8 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
   const long G = (long)p->gnx * p->gny * p->gnz;
   const REAL dt = (REAL)p->dt;
   const REAL hdt = (REAL)(0.5f * p->dt);
+  const int half = p->storage == 1;
+  (void)half;
   if (X <= 0 || Y <= 0 || Z <= 0 || Z > 4096 || P > Z || p->rx <= 0 ||
       p->ry <= 0 || p->rz <= 0)
     return 1;
@@ -116,6 +136,8 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
 #endif
 
   REAL* F = fields ? fields : (REAL*)calloc(6 * N, sizeof(REAL));
+  if (fields)
+    for (long i = 0; i < 6 * N; ++i) F[i] = STORE(F[i]);
   REAL* cb = (REAL*)malloc(3 * N * sizeof(REAL));
   REAL* psi = (REAL*)calloc(4 * (size_t)X * Y * (P > 0 ? P : 1), sizeof(REAL));
   REAL* zc = (REAL*)malloc(6 * (size_t)Z * sizeof(REAL));
@@ -150,7 +172,7 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
         for (int z = 0; z < Z; ++z) {
           const int ez = clampi(z - p->oz, 0, p->rz - 1);
           const REAL e = (REAL)eps[(((long)c * p->rx + ex) * p->ry + ey) * p->rz + ez];
-          cb[c * N + (x * (long)Y + y) * Z + z] = dt / FMA(s, hdt, e);
+          cb[c * N + (x * (long)Y + y) * Z + z] = STORE(dt / FMA(s, hdt, e));
         }
       }
 
@@ -188,17 +210,17 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
             const long pi = (x * (long)Y + y) * P + pz;
             const REAL a = FMA(ch[z], dEy_z, bh[z] * phx[pi]);
             const REAL b = FMA(ch[z], dEx_z, bh[z] * phy[pi]);
-            phx[pi] = a;
-            phy[pi] = b;
+            phx[pi] = STORE(a);
+            phy[pi] = STORE(b);
             zEy = FMA(dEy_z, ikh[z], a);
             zEx = FMA(dEx_z, ikh[z], b);
           } else {
             zEy = dEy_z * ikh[z];
             zEx = dEx_z * ikh[z];
           }
-          Hx[i] = FMA(-dt, dEz_y - zEy, Hx[i]);
-          Hy[i] = FMA(-dt, zEx - dEz_x, Hy[i]);
-          Hz[i] = FMA(-dt, dEy_x - dEx_y, Hz[i]);
+          Hx[i] = STORE(FMA(-dt, dEz_y - zEy, Hx[i]));
+          Hy[i] = STORE(FMA(-dt, zEx - dEz_x, Hy[i]));
+          Hz[i] = STORE(FMA(-dt, dEy_x - dEx_y, Hz[i]));
         }
 
     /* E^{n+1} from H^{n+1/2}, source column values of step n. */
@@ -224,8 +246,8 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
             const long pi = (x * (long)Y + y) * P + pz;
             const REAL a = FMA(ce[z], dHy_z, be[z] * pex[pi]);
             const REAL b = FMA(ce[z], dHx_z, be[z] * pey[pi]);
-            pex[pi] = a;
-            pey[pi] = b;
+            pex[pi] = STORE(a);
+            pey[pi] = STORE(b);
             zHy = FMA(dHy_z, ike[z], a);
             zHx = FMA(dHx_z, ike[z], b);
           } else {
@@ -249,7 +271,7 @@ int SUFFIX(oracle_run)(const oracle_problem* p, const float* eps,
             REAL* E = F + c * N;
             const REAL s = (REAL)mask[((long)c * X + x) * Y + y];
             const REAL r = FMA(-s, E[i], cur[c]);
-            E[i] = FMA(cb[c * N + i], r, E[i]);
+            E[i] = STORE(FMA(cb[c * N + i], r, E[i]));
           }
         }
 

@@ -233,8 +233,11 @@ def projection_weights(omega, output_steps, dt):
   return np.linalg.pinv(_output_phases(omega, output_steps, dt).T)
 
 
-def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
-  """Cached PHASORS plan for the engine arguments ``kw`` of :func:`_setup`."""
+def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False,
+                monitors=None, cache=True):
+  """PHASORS plan for the engine arguments ``kw`` of :func:`_setup`, cached
+  by its static configuration unless ``cache`` is False; ``monitors``
+  (domain-frame ``(origin, shape)`` boxes) replaces the recorded region."""
   eps = kw["epsilon"]
   mask = kw["absorption_mask"]
   domain = (int(mask.shape[1]), int(mask.shape[2]), int(kw["pml_kappa"].shape[0]))
@@ -248,8 +251,8 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
          shape, kw["output_steps"], kw["pml_widths"],
          _key_array(kw["pml_kappa"]), _key_array(kw["pml_sigma"]),
          _key_array(kw["pml_alpha"]), weights.tobytes(), bool(record_h),
-         knobs)
-  plan = cached_plan(key, lambda: engine.Plan(
+         knobs, None if monitors is None else tuple(map(tuple, monitors)))
+  make = lambda: engine.Plan(
       domain=domain, offset=kw["offset"], region=region, tt=tt, dt=kw["dt"],
       pml_widths=kw["pml_widths"], pml_kappa=kw["pml_kappa"],
       pml_sigma=kw["pml_sigma"], pml_alpha=kw["pml_alpha"],
@@ -257,7 +260,8 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False):
       output_steps=kw["output_steps"], out_mode=out_mode, weights=weights,
       record_h=record_h, tile_y=knobs.tile_y, seg_x=knobs.seg_x,
       steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
-      stages=knobs.stages, warps=knobs.warps))
+      stages=knobs.stages, warps=knobs.warps, monitors=monitors)
+  plan = cached_plan(key, make) if cache else make()
   return plan, prof
 
 

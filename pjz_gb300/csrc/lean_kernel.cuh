@@ -416,8 +416,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 }
 
 // (zz, tile_y) shapes of the lean kernel: the streamed kernel's tile heights
-// for these zz with 4 ring stages.
-#define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29)
+// for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
+#define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
 
 template <int ZC, int TYC>
 __global__ void __launch_bounds__(384, 1) yee_lean_kernel(const StreamArgs sa) {

@@ -303,7 +303,8 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
     if (!required) return PJZFDTD_OK;
     return fail(PJZFDTD_ERR_UNSUPPORTED,
                 "the lean kernel needs (zz, tile_y) in {(64, 14), (48, 19), "
-                "(32, 29)} (got (%d, %d)), one step per launch and z-PML widths "
+                "(32, 29), (32, 28)} (got (%d, %d)), one step per launch and "
+                "z-PML widths "
                 "that are multiples of 4 (got %d, %d)",
                 Z, ty, p.pml_lo, p.pml_hi);
   }

@@ -7,10 +7,14 @@ engine's fused adjoint, so pjz code can switch with::
 
     import pjz_gb300.jax_shim as fdtdz_jax
 
-Arrays cross between JAX and torch through DLPack (zero-copy on the same
-GPU) when called eagerly; under ``jax.jit`` the call goes through
-``jax.pure_callback`` (a host round trip of the inputs and outputs).  jax
-is not a dependency: importing this module without jax raises ImportError.
+``fdtdz`` hands arrays between JAX and torch through DLPack (zero-copy on
+the same GPU) when called eagerly; under ``jax.jit`` it goes through
+``jax.pure_callback`` (a host round trip of the inputs and outputs).
+``field``'s forward and backward always run in ``jax.pure_callback``
+(``pjz_gb300/_jax_host.py``), so pjz's jitted ``field`` and ``scatter``
+(``src/pjz/_field.py:171, 403-404``) can call them inside a trace; the
+backward runs the forward again and then one fused adjoint solve.  jax is
+not a dependency: importing this module without jax raises ImportError.
 """
 
 try:
@@ -25,7 +29,7 @@ import numpy as np
 import torch
 import torch.utils.dlpack as tdl
 
-from . import _fdtdz, _field
+from . import _fdtdz, _field, _jax_host
 
 
 def _to_torch(x):
@@ -71,34 +75,33 @@ def fdtdz(**kw):
                            **arrays)
 
 
-def _field_torch(eps, source, omega, pos, sp, need_grad):
-  e = _to_torch(eps)
-  e = (e.cuda() if not e.is_cuda else e).to(torch.float32)
-  if need_grad:
-    e = e.detach().requires_grad_(True)
-  out = _field.field(e, _to_torch(source), np.asarray(omega), pos, sp)
-  return e, out
-
-
 @partial(jax.custom_vjp, nondiff_argnums=(3, 4))
 def field(epsilon, source, omega, source_pos, sim_params):
-  """pjz ``field`` on the engine; differentiable w.r.t. ``epsilon``."""
-  _, out = _field_torch(epsilon, source, omega, source_pos, sim_params, False)
-  return _to_jax(out)
+  """pjz ``field`` on the engine; differentiable w.r.t. ``epsilon`` and
+  usable under ``jax.jit`` (the engine runs in a ``jax.pure_callback``)."""
+  shape = (jnp.shape(omega)[0], 3) + tuple(jnp.shape(epsilon)[1:])
+  return jax.pure_callback(
+      partial(_jax_host.field_host, source_pos=source_pos,
+              sim_params=sim_params),
+      jax.ShapeDtypeStruct(shape, jnp.complex64), epsilon, source, omega)
 
 
 def _field_fwd(epsilon, source, omega, source_pos, sim_params):
-  e, out = _field_torch(epsilon, source, omega, source_pos, sim_params, True)
-  return _to_jax(out.detach()), (e, out)
+  # The residuals are the inputs: the backward callback runs the forward
+  # again before its adjoint solve (a traced function cannot keep torch
+  # tensors between the two callbacks).
+  return field(epsilon, source, omega, source_pos, sim_params), (
+      epsilon, source, omega)
 
 
 def _field_bwd(source_pos, sim_params, res, g):
-  e, out = res
-  # JAX hands the cotangent of a complex output as conj(dL/dz*)-style
-  # ``g``; torch's grad_outputs wants dL/d(conj z) * 2, i.e. conj(g).
-  gt = torch.conj(_to_torch(g).to(out.device))
-  (ge,) = torch.autograd.grad(out, e, grad_outputs=gt)
-  return _to_jax(ge), None, None
+  epsilon, source, omega = res
+  ge = jax.pure_callback(
+      partial(_jax_host.field_vjp_host, source_pos=source_pos,
+              sim_params=sim_params),
+      jax.ShapeDtypeStruct(jnp.shape(epsilon), jnp.float32), epsilon, source,
+      omega, g)
+  return ge, None, None
 
 
 field.defvjp(_field_fwd, _field_bwd)

@@ -118,3 +118,29 @@ def test_negative_output_start_is_allowed(lib):
   # pjz asks for samples before step 0 when tt < 2 * interval * ww + 1.
   p = _plan(output_steps=(-12, 50, 9))
   assert p.num_samples == len(range(-12, 50, 9))
+
+
+@pytest.mark.parametrize("Z", [64, 48, 32])
+@pytest.mark.parametrize("pml", [(8, 8), (4, 4), (0, 0), (4, 8), (12, 4)])
+def test_lean_kernel_plans_resolve(lib, Z, pml):
+  """kernel=3 (lean) resolves on every thin-z shape it is tested with on the
+  GPU: a compile-time tile, one step per launch, interior plus PML warps
+  within the block bound; uneven slab widths are refused."""
+  import sys
+  sys.path.insert(0, os.path.dirname(__file__))
+  from _cases import random_problem
+  case = random_problem(1, X=19, Y=2 * {64: 14, 48: 19, 32: 29}[Z] + 5, Z=Z,
+                        pml=pml, tt=24, steps=(9, 24, 4))
+  kw = dict(domain=case["domain"], offset=case["offset"],
+            region=case["eps"].shape[1:], tt=24, dt=0.5, pml_widths=pml,
+            pml_kappa=case["kappa"], pml_sigma=case["sigma"],
+            pml_alpha=case["alpha"], source_origin=case["source_origin"],
+            source_shape=case["source_profile"].shape[2:], source_ncols=2,
+            output_steps=(9, 24, 4), out_mode=engine.OUT_SNAPSHOTS, kernel=3)
+  cfg = engine.Plan(**kw).launch_config()
+  assert cfg["kernel"] == 3 and cfg["steps_per_pass"] == 1
+  assert (Z, cfg["tile_y"]) in {(64, 14), (48, 19), (32, 29), (32, 28)}
+  assert cfg["threads"] <= 384 and cfg["threads"] % 32 == 0
+  with pytest.raises(NotImplementedError, match="lean"):
+    engine.Plan(**dict(kw, pml_widths=(3, 5), pml_kappa=np.ones((Z, 2)),
+                       pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2))))

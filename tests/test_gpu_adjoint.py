@@ -6,7 +6,10 @@ against central finite differences.
   at interior, region-boundary (edge-extended) and source-plane voxels;
 * c2: the 512x512x64 c1 geometry, objective sum_w |port . E_y(x_out)|^2,
   FD of the GPU FP32 forward along the gradient's sign pattern (1e-3), along
-  a random direction and at single voxels (1e-2, the FP32 noise floor).
+  a random direction and at single voxels (1e-2, the FP32 noise floor);
+  and at 16 seeded single voxels against the tangent-linear derivative
+  (``pjz_gb300._tangent``: the exact directional derivative of the solve,
+  with no difference taken, so FP32 noise does not swamp it), 1e-3.
 Small cases: 1e-3 relative (vector norm over the checked voxels).
 """
 
@@ -18,7 +21,7 @@ import oracle
 from oracle import adjoint as oradj
 from oracle import pjz_ref
 import pjz_gb300
-from pjz_gb300 import workloads
+from pjz_gb300 import _tangent, workloads
 from pjz_gb300._fdtdz import LaunchParams
 
 pytestmark = pytest.mark.gpu
@@ -175,3 +178,44 @@ def test_c2_gradient_vs_finite_differences(native):
   assert err_sign < 1e-3
   assert err_dir < 1e-2
   assert err < 1e-2
+
+
+def test_c2_gradient_vs_tangent_linear_16_voxels(native):
+  """c2's gate at 16 seeded voxels of the 50x50x6 design region.
+
+  A central difference of the FP32 forward at delta-eps 1e-3 carries ~10%
+  rounding noise on these derivatives (see the test above), so the
+  reference here is the tangent-linear derivative of the same solve: one
+  extra solve per voxel, driven at the voxel by the forward's own field
+  increments (checked against FP64 central differences on the CPU in
+  tests/test_tangent_cpu.py).  The adjoint gradient must match it to 1e-3
+  relative (L2 over the 16 voxels)."""
+  wl = workloads.design_c1(tt=20000)
+  eps = torch.tensor(wl.epsilon, device=DEV, requires_grad=True)
+  src = torch.as_tensor(wl.source, device=DEV)
+  port = torch.as_tensor(workloads.port_profile(wl), device=DEV)
+  F = pjz_gb300.field(eps, src, wl.omega, wl.source_pos, wl.sim_params)
+  workloads.overlap_objective(F, wl, port).backward()
+  grad = eps.grad.cpu().numpy()
+
+  rng = np.random.default_rng(1)
+  (bx, by, bz), (nx, ny, nz) = wl.design_box
+  voxels = [(int(rng.integers(3)), bx + int(rng.integers(nx)),
+             by + int(rng.integers(ny)), bz + int(rng.integers(nz)))
+            for _ in range(16)]
+  xo = workloads.output_plane(wl)
+  _, _, yy, zz = wl.epsilon.shape
+  dF = _tangent.field_voxel_jvp(wl.epsilon, src, wl.omega, wl.source_pos,
+                                wl.sim_params, voxels, ((xo, 0, 0), (1, yy, zz)))
+  p = port.to(torch.complex128)
+  ov = (F.detach()[:, 1, xo].to(torch.complex128) * p).sum(dim=(-2, -1))
+  dov = (dF[:, :, 1, 0].to(torch.complex128) * p).sum(dim=(-2, -1))
+  tl = (2 * (torch.conj(ov)[None] * dov).real).sum(dim=-1).cpu().numpy()
+  ad = np.array([grad[v] for v in voxels], np.float64)
+  err = np.linalg.norm(ad - tl) / np.linalg.norm(tl)
+  worst = np.max(np.abs(ad - tl) / np.abs(tl))
+  print(f"c2 16 voxels, adjoint vs tangent-linear: rel-L2 {err:.2e}, worst "
+        f"voxel {worst:.2e}")
+  print("tangent", tl)
+  print("adjoint", ad)
+  assert err < 1e-3
