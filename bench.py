@@ -38,6 +38,7 @@ METRIC = ("Gcell-updates/s and HBM GB/s vs roofline; batched grads/s vs plain "
           "loop at 1e-5 rel-L2")
 UNIT = "Gcell-updates/s"
 BYTES_PER_CELL = 60  # read E(3)+H(3)+coef(3), write E(3)+H(3), FP32
+BYTES_PER_CELL_F16 = 30  # the same 15 values per cell-update, binary16
 
 
 def _args():
@@ -61,6 +62,8 @@ def _args():
   ap.add_argument("--no-cpu", action="store_true")
   ap.add_argument("--no-batched", action="store_true",
                   help="c1: skip the batched c4 S-matrix gradient leg")
+  ap.add_argument("--no-f16", action="store_true",
+                  help="c1: skip the binary16-storage leg")
   ap.add_argument("--kernel", type=int, default=0,
                   help="0 auto, 1 register-marching, 2 streamed")
   ap.add_argument("--stages", type=int, default=0)
@@ -336,6 +339,10 @@ def run_native(args):
               "launch_ms": launch_ms,
               "traffic": None if bpc is None else bpc * cells_per_launch}
 
+  f16 = None
+  if args.workload == "c1" and not args.no_f16:
+    f16 = f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells)
+
   e2e = None
   if not args.no_e2e:
     eps_h = torch.as_tensor(wl.epsilon).pin_memory()
@@ -388,7 +395,7 @@ def run_native(args):
                    "parallelism": "replicas" if world > 1 else "single",
                    "launch": cfg},
         "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
-        "batched": batched,
+        "batched": batched, "reduced_precision": f16,
         # per solve: the step launches of its schedule, the cb and absorber
         # set-up kernels and one record pass per sample step.
         "gpu_launches": args.steps * (plan.step_launches() + 2 + plan.num_samples),
@@ -397,6 +404,54 @@ def run_native(args):
     print(json.dumps(line), flush=True)
   if world > 1:
     torch.distributed.destroy_process_group()
+
+
+def f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells):
+  """The same c1 solve with pjz's use_reduced_precision=True: binary16
+  storage of fields, coefficients and CPML state, FP32 arithmetic (30 B per
+  cell-update instead of 60).  Timed like the main line (W warm-up solves,
+  K timed, device-resident), plus its step-kernel launch time against the
+  HBM roofline on the 30 B figure."""
+  import torch
+  from pjz_gb300 import _field
+  sp = wl.sim_params._replace(use_reduced_precision=True)
+  kw, omega = _field._setup(eps, src, wl.omega, wl.source_pos, sp)
+  plan, prof = _field.phasor_plan(kw, omega)
+  run_args = dict(epsilon=eps, absorption_mask=kw["absorption_mask"],
+                  source=prof, waveform=kw["source_waveform"])
+  out = torch.empty(plan.out_shape(), dtype=torch.float32, device=eps.device)
+  for _ in range(args.warmup):
+    plan.run(**run_args, out=out)
+  barrier()
+  e0, e1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+  e0.record(stream)
+  for _ in range(args.steps):
+    plan.run(**run_args, out=out)
+  e1.record(stream)
+  barrier()
+  ms = maxed(e0.elapsed_time(e1)) / args.steps
+  nl = min(sp.tt - 1, 2000)
+  k0, k1 = (torch.cuda.Event(enable_timing=True) for _ in range(2))
+  k0.record(stream)
+  plan.run(**run_args, out=out, steps=(1, 1 + nl))
+  k1.record(stream)
+  torch.cuda.synchronize()
+  launch_ms = k0.elapsed_time(k1) / plan.step_launches(1, 1 + nl)
+  per_launch = int(np.prod(wl.domain))
+  achieved = BYTES_PER_CELL_F16 * per_launch / (launch_ms / 1e3) / 1e9
+  peak, peak_kind = _peaks()
+  return {"value": world * cells / (ms / 1e3) / 1e9, "unit": UNIT,
+          "ms_per_step": ms, "dtype": "binary16 storage, f32 arithmetic",
+          "launch": plan.launch_config(),
+          "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                       "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": f"hbm_gbs of {peak_kind}",
+                       "kernel": "yee_lean_kernel (binary16)",
+                       "algorithmic_bytes_per_launch": BYTES_PER_CELL_F16 * per_launch,
+                       "launch_ms": launch_ms},
+          "accuracy": "rel-L2 vs the FP64 oracle: asserted and printed by "
+                      "tests/test_gpu_f16.py (c0) and "
+                      "tests/test_gpu_full_length.py (c1)"}
 
 
 def batched_c4(device_index, clock_path):

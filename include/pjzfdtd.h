@@ -15,8 +15,8 @@
  *   pml_widths                      -> pml_lo, pml_hi
  *   output_steps (start,stop,step)  -> out_start, out_stop, out_step
  *   offset (px,py,pz)               -> ox, oy, oz
- *   use_reduced_precision           -> only FP32 storage is implemented;
- *                                      the flag stays with pjz's z budget
+ *   use_reduced_precision           -> storage (binary16 fields, FP32
+ *                                      arithmetic) and pjz's z budget
  *   launch_params                   -> tile_y, seg_x (0 = autotuned)
  *
  * fdtdz's plane sources map onto the general source box: an x-normal source
@@ -44,7 +44,7 @@
 extern "C" {
 #endif
 
-#define PJZFDTD_ABI_VERSION 1
+#define PJZFDTD_ABI_VERSION 2
 
 typedef enum {
   PJZFDTD_OK = 0,
@@ -68,6 +68,18 @@ typedef enum {
   PJZFDTD_OUT_GRADIENT = 3
 } pjzfdtd_out_mode;
 
+typedef enum {
+  /* E, H, the E-update coefficient and the z-PML state stored as FP32. */
+  PJZFDTD_STORAGE_F32 = 0,
+  /* Stored as IEEE binary16 (rounded to nearest even on every write), with
+     all arithmetic, source sums and phasor accumulators in FP32: half the
+     HBM bytes per cell-update.  fdtdz's use_reduced_precision
+     (src/pjz/_field.py:52, pjz's default) selects 16-bit storage; this is
+     that mode.  Served by the lean streamed kernel (kernel 3), one step per
+     launch, zz in {64, 48, 32} and z-PML widths that are multiples of 4. */
+  PJZFDTD_STORAGE_F16 = 1
+} pjzfdtd_storage;
+
 typedef struct pjzfdtd_problem {
   int32_t xx, yy, zz;          /* simulation domain in cells */
   int32_t ox, oy, oz;          /* fdtdz `offset` of the epsilon region */
@@ -86,7 +98,8 @@ typedef struct pjzfdtd_problem {
   int32_t seg_x;               /* launch params: x planes per CTA, 0 = auto */
   int32_t steps_per_pass;      /* launch params: time steps per HBM pass, 0 = auto */
   int32_t kernel;              /* launch params: 0 auto, 1 register-marching,
-                                  2 bulk-copy streamed (needs zz % 4 == 0) */
+                                  2 bulk-copy streamed (needs zz % 4 == 0),
+                                  3 lean streamed (compile-time zz/tile_y) */
   int32_t stages;              /* launch params: streamed ring depth, 0 = auto */
   int32_t warps;               /* launch params: streamed compute warps per CTA,
                                   0 = auto (one row per warp and pass) */
@@ -95,6 +108,7 @@ typedef struct pjzfdtd_problem {
   int32_t test_stall_bytes;    /* test hook, 0 in use: the streamed producer
                                   announces this many bytes more than it
                                   copies, so waits run out (no fault) */
+  int32_t storage;             /* pjzfdtd_storage of the state (ABI 2) */
 } pjzfdtd_problem;
 
 typedef struct pjzfdtd_buffers {

@@ -200,13 +200,18 @@ def extend_epsilon(eps: torch.Tensor, domain: Sequence[int], offset) -> torch.Te
 
 def fold_to_region(grad: torch.Tensor, region, offset) -> torch.Tensor:
   """Adjoint of :func:`extend_epsilon`: sums domain gradients onto the
-  region cell each domain cell copies."""
+  region cell each domain cell copies.  Along each axis the cells below the
+  region fold onto its first cell and those above onto its last; the sums
+  are plain reductions (no atomics), so the result is deterministic."""
   out = grad
-  for ax, (n, o, s) in enumerate(zip(grad.shape[1:], offset, region)):
-    idx = torch.clamp(torch.arange(n, device=grad.device) - o, 0, s - 1)
-    shape = list(out.shape)
-    shape[ax + 1] = s
-    acc = torch.zeros(shape, dtype=out.dtype, device=out.device)
-    acc.index_add_(ax + 1, idx, out)
-    out = acc
+  for ax, (o, s) in enumerate(zip(offset, region)):
+    d = ax + 1
+    n = out.shape[d]
+    mid = out.narrow(d, o, s).clone()
+    if o > 0:
+      mid.narrow(d, 0, 1).add_(out.narrow(d, 0, o).sum(dim=d, keepdim=True))
+    if o + s < n:
+      mid.narrow(d, s - 1, 1).add_(
+          out.narrow(d, o + s, n - o - s).sum(dim=d, keepdim=True))
+    out = mid
   return out

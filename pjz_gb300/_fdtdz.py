@@ -89,8 +89,9 @@ def fdtdz(
 
   The domain is ``absorption_mask.shape[1:]`` in x, y and
   ``pml_kappa.shape[0]`` in z; ``epsilon`` sits at ``offset`` inside it and is
-  edge-extended outside.  ``use_reduced_precision`` is accepted for
-  compatibility; fields are always stored and updated in FP32.
+  edge-extended outside.  ``use_reduced_precision`` selects binary16
+  storage of the fields, coefficients and CPML state with FP32 arithmetic
+  (fdtdz's 16-bit mode); False stores FP32.
   """
   dev = device or (epsilon.device if isinstance(epsilon, torch.Tensor)
                    and epsilon.is_cuda else torch.device("cuda"))
@@ -116,7 +117,7 @@ def fdtdz(
   region = tuple(int(v) for v in eps.shape[1:])
   key = ("fdtdz", domain, region, tuple(offset), tt, float(dt), origin, shape,
          steps, tuple(pml_widths), _key_array(pml_kappa), _key_array(pml_sigma),
-         _key_array(pml_alpha), knobs)
+         _key_array(pml_alpha), knobs, bool(use_reduced_precision))
   plan = cached_plan(key, lambda: engine.Plan(
       domain=domain, offset=offset, region=region, tt=tt, dt=dt,
       pml_widths=pml_widths, pml_kappa=pml_kappa, pml_sigma=pml_sigma,
@@ -124,7 +125,8 @@ def fdtdz(
       source_ncols=2, output_steps=steps, out_mode=engine.OUT_SNAPSHOTS,
       tile_y=knobs.tile_y, seg_x=knobs.seg_x,
       steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
-      stages=knobs.stages, warps=knobs.warps))
+      stages=knobs.stages, warps=knobs.warps,
+      storage=engine.STORAGE_F16 if use_reduced_precision else engine.STORAGE_F32))
   out, _ = plan.run(epsilon=eps, absorption_mask=mask, source=prof,
                     waveform=wave)
   return out

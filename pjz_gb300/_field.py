@@ -246,12 +246,14 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False,
   tt = int(kw["source_waveform"].shape[0])
   weights = projection_weights(omega, kw["output_steps"], kw["dt"])
   knobs = launch_knobs(kw["launch_params"])
+  storage = storage_of(kw)
   region = tuple(int(v) for v in eps.shape[1:])
   key = ("field", domain, region, kw["offset"], tt, float(kw["dt"]), origin,
          shape, kw["output_steps"], kw["pml_widths"],
          _key_array(kw["pml_kappa"]), _key_array(kw["pml_sigma"]),
          _key_array(kw["pml_alpha"]), weights.tobytes(), bool(record_h),
-         knobs, None if monitors is None else tuple(map(tuple, monitors)))
+         knobs, None if monitors is None else tuple(map(tuple, monitors)),
+         storage)
   make = lambda: engine.Plan(
       domain=domain, offset=kw["offset"], region=region, tt=tt, dt=kw["dt"],
       pml_widths=kw["pml_widths"], pml_kappa=kw["pml_kappa"],
@@ -260,9 +262,17 @@ def phasor_plan(kw, omega, out_mode=engine.OUT_PHASORS, record_h=False,
       output_steps=kw["output_steps"], out_mode=out_mode, weights=weights,
       record_h=record_h, tile_y=knobs.tile_y, seg_x=knobs.seg_x,
       steps_per_pass=knobs.steps_per_pass, kernel=knobs.kernel,
-      stages=knobs.stages, warps=knobs.warps, monitors=monitors)
+      stages=knobs.stages, warps=knobs.warps, monitors=monitors,
+      storage=storage)
   plan = cached_plan(key, make) if cache else make()
   return plan, prof
+
+
+def storage_of(kw):
+  """Engine storage for pjz's ``use_reduced_precision`` (``_field.py:52``):
+  fdtdz's reduced precision is 16-bit storage, so True selects binary16
+  fields with FP32 arithmetic, False FP32 throughout."""
+  return engine.STORAGE_F16 if kw["use_reduced_precision"] else engine.STORAGE_F32
 
 
 def _launch_dict(launch_params):
@@ -336,7 +346,7 @@ class _FieldFn(torch.autograd.Function):
         absorption_mask=kw["absorption_mask"], pml_widths=kw["pml_widths"],
         pml_kappa=kw["pml_kappa"], pml_sigma=kw["pml_sigma"],
         pml_alpha=kw["pml_alpha"], src_term=src_term,
-        launch=_launch_dict(kw["launch_params"]))
+        launch=dict(_launch_dict(kw["launch_params"]), storage=storage_of(kw)))
     return _adjoint.fold_to_region(grad, ctx.region, ctx.offset), None, None, None, None
 
 

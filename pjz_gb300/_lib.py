@@ -11,6 +11,7 @@ from . import _build
 
 OK, ERR_INVALID, ERR_CUDA, ERR_WORKSPACE, ERR_TIMEOUT, ERR_UNSUPPORTED = range(6)
 OUT_NONE, OUT_SNAPSHOTS, OUT_PHASORS, OUT_GRADIENT = range(4)
+STORAGE_F32, STORAGE_F16 = range(2)
 MAX_ROWS = 32
 
 _PROBLEM_INTS = (
@@ -21,7 +22,7 @@ _PROBLEM_INTS2 = (
     "out_start", "out_stop", "out_step", "out_mode", "out_rows", "record_h",
     "grad_x0", "grad_y0", "grad_z0", "grad_nx", "grad_ny", "grad_nz",
     "tile_y", "seg_x", "steps_per_pass", "kernel", "stages", "warps",
-    "wait_limit_kcycles", "test_stall_bytes")
+    "wait_limit_kcycles", "test_stall_bytes", "storage")
 
 
 class Problem(ctypes.Structure):

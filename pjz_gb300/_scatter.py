@@ -123,7 +123,7 @@ def _plane_phasors(epsilon, solves, planes):
     plans.append((plan, om_arr.shape[0]))
     inputs.append(dict(epsilon=epsilon, absorption_mask=kw["absorption_mask"],
                        source=prof, waveform=kw["source_waveform"]))
-  outs = engine.Batch([pl for pl, _ in plans]).run(inputs, graph=False)
+  outs = engine.run_many([pl for pl, _ in plans], inputs)
   res = []
   for (plan, ww), (out, _) in zip(plans, outs):
     views = plan.split(out)

@@ -78,7 +78,8 @@ def field_voxel_jvp(epsilon, source, omega, source_pos: int,
   (mo, ms) = monitor
   mbox = (tuple(int(o) + off[ax] for ax, o in enumerate(mo)),
           tuple(int(s) for s in ms))
-  knobs = _field._launch_dict(kw["launch_params"])
+  knobs = dict(_field._launch_dict(kw["launch_params"]),
+               storage=_field.storage_of(kw))
   base = dict(domain=domain, offset=off, region=region, tt=tt, dt=dt,
               pml_widths=kw["pml_widths"], pml_kappa=kw["pml_kappa"],
               pml_sigma=kw["pml_sigma"], pml_alpha=kw["pml_alpha"], **knobs)
@@ -109,7 +110,7 @@ def field_voxel_jvp(epsilon, source, omega, source_pos: int,
     inputs.append(dict(epsilon=eps, absorption_mask=mask, source=u,
                        waveform=wave))
   ww = om.shape[0]
-  outs = engine.Batch(plans).run(inputs, graph=False)
+  outs = engine.run_many(plans, inputs)
   res = []
   for plan, (out, _) in zip(plans, outs):
     v = plan.split(out)[0]

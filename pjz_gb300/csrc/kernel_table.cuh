@@ -27,9 +27,9 @@ BatchKernel batch2_kernel_ptr();
 inline BatchKernel batch_kernel_ptr(int steps) {
   return steps == 2 ? batch2_kernel_ptr() : batch1_kernel_ptr();
 }
-// Lean single-step streamed kernel for (zz, tile_y) (kern_lean.cu), or
-// nullptr when no compile-time shape matches.
-StreamKernel lean_kernel_ptr(int zz, int tile_y);
+// Lean single-step streamed kernel for (zz, tile_y) and storage (0 FP32,
+// 1 binary16) (kern_lean.cu), or nullptr when no compile-time shape matches.
+StreamKernel lean_kernel_ptr(int zz, int tile_y, int storage);
 // Block size bound of the lean kernel.
 constexpr int kLeanThreads = 384;
 // Permittivity rendering kernel (kern_render.cu).

@@ -24,6 +24,9 @@
 // Barriers and bounded waits follow the streamed kernel's protocol.
 #pragma once
 
+#include <cuda_fp16.h>
+#include <string.h>
+
 #include "stream_kernel.cuh"
 #include "kernel_table.cuh"
 
@@ -44,39 +47,115 @@ __host__ __device__ inline int lean_warps_pml(int ty, int plo, int phi) {
   return ((ty + 1) * lean_quads_pml(plo, phi) + 31) / 32;
 }
 
-__device__ __forceinline__ float4 lds4(const float* p) {
-  return *reinterpret_cast<const float4*>(p);
-}
-__device__ __forceinline__ void sts4(float* p, const float v[4]) {
-  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
-}
-__device__ __forceinline__ void unpack4(const float4 v, float o[4]) {
-  o[0] = v.x;
-  o[1] = v.y;
-  o[2] = v.z;
-  o[3] = v.w;
-}
+// Shared-memory geometry of one lean CTA for storage type T (bytes).  The
+// ring slot holds E rows -1..TY, H rows -1..TY-1, E-coefficient rows
+// 0..TY-1 (all T), the absorber window (FP32) and the z-PML state rows (T,
+// row stride Pp = P rounded up to 16 bytes); every region starts on a
+// 16-byte boundary, as the bulk copies need.  After the ring: new H
+// [2][3][RH*Z], new E [2][3][TY*Z], new PML state [2][4][TY*Pp] (T), then
+// the mbarriers.  For T = float this is StreamGeom's layout.
+template <typename T>
+struct LeanGeom {
+  int TY, Z, Pp, RE, RH, MT;
+  int e_off, h_off, c_off, m_off, p_off, stage;  // bytes within a slot
+  __host__ __device__ LeanGeom(int ty, int z, int p) {
+    constexpr int per16 = 16 / (int)sizeof(T);
+    TY = ty;
+    Z = z;
+    Pp = (p + per16 - 1) / per16 * per16;
+    RE = ty + 2;
+    RH = ty + 1;
+    MT = round4(ty) + 8;
+    e_off = 0;
+    h_off = e_off + 3 * RE * z * (int)sizeof(T);
+    c_off = h_off + 3 * RH * z * (int)sizeof(T);
+    m_off = c_off + 3 * ty * z * (int)sizeof(T);
+    p_off = m_off + 3 * MT * 4;
+    stage = p_off + 4 * RH * Pp * (int)sizeof(T);
+  }
+  __host__ __device__ size_t hn_bytes() const { return 2 * 3 * (size_t)RH * Z * sizeof(T); }
+  __host__ __device__ size_t en_bytes() const { return 2 * 3 * (size_t)TY * Z * sizeof(T); }
+  __host__ __device__ size_t pn_bytes() const { return 2 * 4 * (size_t)TY * Pp * sizeof(T); }
+  __host__ __device__ size_t bytes(int stages) const {
+    return (size_t)stages * stage + hn_bytes() + en_bytes() + pn_bytes() +
+           (size_t)(2 * stages + 2) * sizeof(uint64_t) + 16;
+  }
+};
+
+// Four consecutive stored values to FP32 and back (128-bit accesses for
+// float, 64-bit for binary16; conversions to binary16 round to nearest
+// even, widening is exact).
+template <typename T>
+struct Quad;
+template <>
+struct Quad<float> {
+  static __device__ __forceinline__ void ld(const float* p, float o[4]) {
+    const float4 v = *reinterpret_cast<const float4*>(p);
+    o[0] = v.x;
+    o[1] = v.y;
+    o[2] = v.z;
+    o[3] = v.w;
+  }
+  static __device__ __forceinline__ void st(float* p, const float v[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+  static __device__ __forceinline__ float ld1(const float* p) { return *p; }
+};
+template <>
+struct Quad<__half> {
+  static __device__ __forceinline__ void ld(const __half* p, float o[4]) {
+    const uint2 u = *reinterpret_cast<const uint2*>(p);
+    __half2 lo, hi;
+    memcpy(&lo, &u.x, 4);
+    memcpy(&hi, &u.y, 4);
+    const float2 a = __half22float2(lo), b = __half22float2(hi);
+    o[0] = a.x;
+    o[1] = a.y;
+    o[2] = b.x;
+    o[3] = b.y;
+  }
+  static __device__ __forceinline__ void st(__half* p, const float v[4]) {
+    const __half2 lo = __floats2half2_rn(v[0], v[1]);
+    const __half2 hi = __floats2half2_rn(v[2], v[3]);
+    uint2 u;
+    memcpy(&u.x, &lo, 4);
+    memcpy(&u.y, &hi, 4);
+    *reinterpret_cast<uint2*>(p) = u;
+  }
+  static __device__ __forceinline__ float ld1(const __half* p) {
+    return __half2float(*p);
+  }
+};
 
 // One CTA of the lean kernel: tile `tile` of y rows, segment `seg` of x
-// planes.  ZC / TYC: zz and tile_y (compile-time).
-template <int ZC, int TYC>
+// planes.  ZC / TYC: zz and tile_y (compile-time); T: storage type of the
+// fields, coefficients and z-PML state in HBM and shared memory (float, or
+// __half for reduced-precision storage); arithmetic is FP32 either way.
+template <int ZC, int TYC, typename T>
 __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int seg,
-                                          float* sm) {
+                                          unsigned char* sm) {
+  using Q = Quad<T>;
   constexpr int Z = ZC, TY = TYC;
   constexpr int RE = TY + 2, RH = TY + 1;
   constexpr int REZ = RE * Z, RHZ = RH * Z, TYZ = TY * Z;
+  constexpr uint32_t ES = sizeof(T);
   const StepArgs& a = sa.s;
   const int X = a.X, Y = a.Y;
   const int S = sa.stages;
-  const StreamGeom g(TY, Z, a.plo + a.phi, 0);
+  const LeanGeom<T> g(TY, Z, a.plo + a.phi);
   const int Pp = g.Pp;
-  float* hn = sm + (size_t)S * g.stage;   // [2][3][RH*Z]
-  float* en = hn + g.hn_floats();         // [2][3][TY*Z]
-  float* pn = en + g.en_floats();         // [2][4][TY*Pp]
-  uint64_t* full = reinterpret_cast<uint64_t*>(pn + g.pn_floats());
+  T* hn = reinterpret_cast<T*>(sm + (size_t)S * g.stage);  // [2][3][RH*Z]
+  T* en = hn + 2 * 3 * RHZ;                                // [2][3][TY*Z]
+  T* pn = en + 2 * 3 * TYZ;                                // [2][4][TY*Pp]
+  uint64_t* full = reinterpret_cast<uint64_t*>(pn + 2 * 4 * TY * Pp);
   uint64_t* done = full + S;
   uint64_t* freeb = done + S;
   __shared__ int abort_flag;
+  const T* fin = reinterpret_cast<const T*>(a.fin);
+  T* fout = reinterpret_cast<T*>(a.fout);
+  const T* cbg = reinterpret_cast<const T*>(a.cb);
+  const T* psi_in = reinterpret_cast<const T*>(a.psi_in);
+  T* psi_out = reinterpret_cast<T*>(a.psi_out);
 
   const int tid = threadIdx.x;
   const int ncomp = blockDim.x - 32;
@@ -108,10 +187,12 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     mbar_init(&freeb[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (size_t i = tid; i < (size_t)S * g.stage + g.hn_floats() + g.en_floats() +
-                               g.pn_floats();
-       i += blockDim.x)
-    sm[i] = 0.f;
+  {
+    uint32_t* w = reinterpret_cast<uint32_t*>(sm);
+    const size_t nw = ((size_t)S * g.stage + g.hn_bytes() + g.en_bytes() +
+                       g.pn_bytes()) / 4;
+    for (size_t i = tid; i < nw; i += blockDim.x) w[i] = 0u;
+  }
   fence_async_smem();
   __syncthreads();
 
@@ -119,32 +200,37 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     if ((tid & 31) != 0) return;
     // ---------------- producer (one lane) ----------------
     auto fill = [&](int xp, int slot, bool fullp) {
-      float* st = sm + (size_t)slot * g.stage;
-      const uint32_t eb = (uint32_t)((ey_hi - ey_lo) * Z * 4);
-      const uint32_t hb = (uint32_t)((hy_hi - ey_lo) * Z * 4);
-      const uint32_t cbb = (uint32_t)(nrows * Z * 4);
+      unsigned char* st = sm + (size_t)slot * g.stage;
+      const uint32_t eb = (uint32_t)((ey_hi - ey_lo) * Z) * ES;
+      const uint32_t hb = (uint32_t)((hy_hi - ey_lo) * Z) * ES;
+      const uint32_t cbb = (uint32_t)(nrows * Z) * ES;
       const uint32_t mbb = (uint32_t)((mb - ma) * 4);
-      const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp * 4);
+      const uint32_t pb = (uint32_t)((hy_hi - ey_lo) * Pp) * ES;
       const uint32_t total = sa.stall_bytes + 3 * eb +
           (fullp ? 3 * (hb + cbb + mbb) + (Pp > 0 ? 4 * pb : 0) : 0);
       mbar_expect_tx(&full[slot], total);
       const long long base = (long long)xp * YZ;
+      T* se = reinterpret_cast<T*>(st + g.e_off);
+      T* sh = reinterpret_cast<T*>(st + g.h_off);
+      T* sc = reinterpret_cast<T*>(st + g.c_off);
+      float* smk = reinterpret_cast<float*>(st + g.m_off);
+      T* sp = reinterpret_cast<T*>(st + g.p_off);
       for (int c = 0; c < 3; ++c)
-        bulk_g2s(st + g.e_off + c * REZ + erow0 * Z,
-                 a.fin + c * N + base + (long long)ey_lo * Z, eb, &full[slot]);
+        bulk_g2s(se + c * REZ + erow0 * Z,
+                 fin + c * N + base + (long long)ey_lo * Z, eb, &full[slot]);
       if (!fullp) return;
       for (int c = 0; c < 3; ++c) {
-        bulk_g2s(st + g.h_off + c * RHZ + erow0 * Z,
-                 a.fin + (3 + c) * N + base + (long long)ey_lo * Z, hb, &full[slot]);
-        bulk_g2s(st + g.c_off + c * TYZ, a.cb + c * N + base + (long long)y0 * Z,
-                 cbb, &full[slot]);
-        bulk_g2s(st + g.m_off + c * g.MT,
+        bulk_g2s(sh + c * RHZ + erow0 * Z,
+                 fin + (3 + c) * N + base + (long long)ey_lo * Z, hb, &full[slot]);
+        bulk_g2s(sc + c * TYZ, cbg + c * N + base + (long long)y0 * Z, cbb,
+                 &full[slot]);
+        bulk_g2s(smk + c * g.MT,
                  sa.mask_ws + ((long long)xp * 3 + c) * sa.Yp + ma, mbb, &full[slot]);
       }
       if (Pp > 0)
         for (int c = 0; c < 4; ++c)
-          bulk_g2s(st + g.p_off + c * RH * Pp + erow0 * Pp,
-                   a.psi_in + c * PXY + ((long long)xp * Y + ey_lo) * Pp, pb,
+          bulk_g2s(sp + c * RH * Pp + erow0 * Pp,
+                   psi_in + c * PXY + ((long long)xp * Y + ey_lo) * Pp, pb,
                    &full[slot]);
     };
     int nfill = 0;  // planes issued so far (x0 + nfill is the next one)
@@ -162,20 +248,20 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
                               sa.wait_cycles);
       if (!ok) break;
       if (x >= xs) {
-        float* hcur = hn + (size_t)b * 3 * RHZ;
-        float* ecur = en + (size_t)b * 3 * TYZ;
-        float* pcur = pn + (size_t)b * 4 * TY * Pp;
+        T* hcur = hn + (size_t)b * 3 * RHZ;
+        T* ecur = en + (size_t)b * 3 * TYZ;
+        T* pcur = pn + (size_t)b * 4 * TY * Pp;
         const long long base = (long long)x * YZ + (long long)y0 * Z;
-        const uint32_t fb = (uint32_t)(nrows * Z * 4);
+        const uint32_t fb = (uint32_t)(nrows * Z) * ES;
         for (int c = 0; c < 3; ++c) {
-          bulk_s2g(a.fout + (3 + c) * N + base, hcur + c * RHZ + Z, fb);
-          bulk_s2g(a.fout + c * N + base, ecur + c * TYZ, fb);
+          bulk_s2g(fout + (3 + c) * N + base, hcur + c * RHZ + Z, fb);
+          bulk_s2g(fout + c * N + base, ecur + c * TYZ, fb);
         }
         if (Pp > 0) {
-          const uint32_t pb = (uint32_t)(nrows * Pp * 4);
+          const uint32_t pb = (uint32_t)(nrows * Pp) * ES;
           const long long pbase = ((long long)x * Y + y0) * Pp;
           for (int c = 0; c < 4; ++c)
-            bulk_s2g(a.psi_out + c * PXY + pbase, pcur + c * TY * Pp, pb);
+            bulk_s2g(psi_out + c * PXY + pbase, pcur + c * TY * Pp, pb);
         }
         bulk_commit();
       }
@@ -257,41 +343,41 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
                               &abort_flag, sa.wait_cycles);
 
-    const float* st = sm + (size_t)slot * g.stage;
-    const float* Es = st + g.e_off;
-    const float* E1 = sm + (size_t)slot1 * g.stage + g.e_off;
-    const float* Hs = st + g.h_off;
-    const float* Cs = st + g.c_off;
-    const float* Ms = st + g.m_off + moff;
-    const float* Ps = st + g.p_off;
-    float* hcur = hn + (size_t)b * 3 * RHZ;
-    const float* hprev = hn + (size_t)(b ^ 1) * 3 * RHZ;
-    float* ecur = en + (size_t)b * 3 * TYZ;
-    float* pcur = pn + (size_t)b * 4 * TY * Pp;
+    const unsigned char* st = sm + (size_t)slot * g.stage;
+    const T* Es = reinterpret_cast<const T*>(st + g.e_off);
+    const T* E1 = reinterpret_cast<const T*>(sm + (size_t)slot1 * g.stage + g.e_off);
+    const T* Hs = reinterpret_cast<const T*>(st + g.h_off);
+    const T* Cs = reinterpret_cast<const T*>(st + g.c_off);
+    const float* Ms = reinterpret_cast<const float*>(st + g.m_off) + moff;
+    const T* Ps = reinterpret_cast<const T*>(st + g.p_off);
+    T* hcur = hn + (size_t)b * 3 * RHZ;
+    const T* hprev = hn + (size_t)(b ^ 1) * 3 * RHZ;
+    T* ecur = en + (size_t)b * 3 * TYZ;
+    T* pcur = pn + (size_t)b * 4 * TY * Pp;
 
     // H^{n+1/2}(x) of the quad at buffer row rH (y = y0 - 1 + rH).
     if (ok && doH) {
       float ex[4], ey[4], ez[4], exy[4], ezy[4], e1y[4], e1z[4], ho[3][4];
-      unpack4(lds4(Es + ieH), ex);
-      unpack4(lds4(Es + REZ + ieH), ey);
-      unpack4(lds4(Es + 2 * REZ + ieH), ez);
-      unpack4(lds4(Es + ieH + Z), exy);
-      unpack4(lds4(Es + 2 * REZ + ieH + Z), ezy);
-      const float exz = zhi ? Es[ieH + 4] : 0.f;
-      const float eyz = zhi ? Es[REZ + ieH + 4] : 0.f;
+      Q::ld(Es + ieH, ex);
+      Q::ld(Es + REZ + ieH, ey);
+      Q::ld(Es + 2 * REZ + ieH, ez);
+      Q::ld(Es + ieH + Z, exy);
+      Q::ld(Es + 2 * REZ + ieH + Z, ezy);
+      const float exz = zhi ? Q::ld1(Es + ieH + 4) : 0.f;
+      const float eyz = zhi ? Q::ld1(Es + REZ + ieH + 4) : 0.f;
       if (has_x1) {
-        unpack4(lds4(E1 + REZ + ieH), e1y);
-        unpack4(lds4(E1 + 2 * REZ + ieH), e1z);
+        Q::ld(E1 + REZ + ieH, e1y);
+        Q::ld(E1 + 2 * REZ + ieH, e1z);
       } else {
 #pragma unroll
         for (int j = 0; j < 4; ++j) e1y[j] = e1z[j] = 0.f;
       }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) unpack4(lds4(Hs + c * RHZ + ieH), ho[c]);
+      for (int c = 0; c < 3; ++c) Q::ld(Hs + c * RHZ + ieH, ho[c]);
       float pa[4], pb[4];
       if (pml) {
-        unpack4(lds4(Ps + pH), pa);
-        unpack4(lds4(Ps + RH * Pp + pH), pb);
+        Q::ld(Ps + pH, pa);
+        Q::ld(Ps + RH * Pp + pH, pb);
       }
       float hx[4], hy[4], hz[4];
 #pragma unroll
@@ -317,12 +403,12 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         hy[j] = ffma(mdt, fsub(zEx, dEz_x), ho[1][j]);
         hz[j] = ffma(mdt, fsub(dEy_x, dEx_y), ho[2][j]);
       }
-      sts4(hcur + ieH, hx);
-      sts4(hcur + RHZ + ieH, hy);
-      sts4(hcur + 2 * RHZ + ieH, hz);
+      Q::st(hcur + ieH, hx);
+      Q::st(hcur + RHZ + ieH, hy);
+      Q::st(hcur + 2 * RHZ + ieH, hz);
       if (pml && rH > 0) {
-        sts4(pcur + (rH - 1) * Pp + col, pa);
-        sts4(pcur + TY * Pp + (rH - 1) * Pp + col, pb);
+        Q::st(pcur + (rH - 1) * Pp + col, pa);
+        Q::st(pcur + TY * Pp + (rH - 1) * Pp + col, pb);
       }
     }
     compute_sync(ncomp);
@@ -331,25 +417,25 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     // E^{n+1}(x) of the quad at tile row rH (y = y0 + rH).
     if (x >= xs && doE) {
       float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4], eo[3][4], cb[3][4];
-      unpack4(lds4(hcur + ihE), hx);
-      unpack4(lds4(hcur + RHZ + ihE), hy);
-      unpack4(lds4(hcur + 2 * RHZ + ihE), hz);
-      unpack4(lds4(hcur + ihE - Z), hxm);
-      unpack4(lds4(hcur + 2 * RHZ + ihE - Z), hzm);
-      const float hxz = zlo ? hcur[ihE - 1] : 0.f;
-      const float hyz = zlo ? hcur[RHZ + ihE - 1] : 0.f;
-      unpack4(lds4(hprev + RHZ + ihE), hyp);
-      unpack4(lds4(hprev + 2 * RHZ + ihE), hzp);
+      Q::ld(hcur + ihE, hx);
+      Q::ld(hcur + RHZ + ihE, hy);
+      Q::ld(hcur + 2 * RHZ + ihE, hz);
+      Q::ld(hcur + ihE - Z, hxm);
+      Q::ld(hcur + 2 * RHZ + ihE - Z, hzm);
+      const float hxz = zlo ? Q::ld1(hcur + ihE - 1) : 0.f;
+      const float hyz = zlo ? Q::ld1(hcur + RHZ + ihE - 1) : 0.f;
+      Q::ld(hprev + RHZ + ihE, hyp);
+      Q::ld(hprev + 2 * RHZ + ihE, hzp);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        unpack4(lds4(Es + c * REZ + ihE), eo[c]);
-        unpack4(lds4(Cs + c * TYZ + icE), cb[c]);
+        Q::ld(Es + c * REZ + ihE, eo[c]);
+        Q::ld(Cs + c * TYZ + icE, cb[c]);
       }
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
       float pa[4], pb[4];
       if (pml) {
-        unpack4(lds4(Ps + 2 * RH * Pp + pE), pa);
-        unpack4(lds4(Ps + 3 * RH * Pp + pE), pb);
+        Q::ld(Ps + 2 * RH * Pp + pE, pa);
+        Q::ld(Ps + 3 * RH * Pp + pE, pb);
       }
       const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
       float enew[3][4];
@@ -394,10 +480,10 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         }
       }
 #pragma unroll
-      for (int c = 0; c < 3; ++c) sts4(ecur + c * TYZ + icE, enew[c]);
+      for (int c = 0; c < 3; ++c) Q::st(ecur + c * TYZ + icE, enew[c]);
       if (pml) {
-        sts4(pcur + 2 * TY * Pp + rH * Pp + col, pa);
-        sts4(pcur + 3 * TY * Pp + rH * Pp + col, pb);
+        Q::st(pcur + 2 * TY * Pp + rH * Pp + col, pa);
+        Q::st(pcur + 3 * TY * Pp + rH * Pp + col, pb);
       }
     }
     // Publish this plane's results to the producer and release its slot.
@@ -419,10 +505,10 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 // for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
 #define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
 
-template <int ZC, int TYC>
+template <int ZC, int TYC, typename T>
 __global__ void __launch_bounds__(384, 1) yee_lean_kernel(const StreamArgs sa) {
-  extern __shared__ __align__(16) float sm[];
-  lean_tile<ZC, TYC>(sa, blockIdx.x, blockIdx.y, sm);
+  extern __shared__ __align__(16) unsigned char lean_sm[];
+  lean_tile<ZC, TYC, T>(sa, blockIdx.x, blockIdx.y, lean_sm);
 }
 
 }  // namespace pjzfdtd

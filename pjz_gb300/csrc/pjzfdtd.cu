@@ -64,6 +64,7 @@ struct pjzfdtd_plan {
   // Resolved launch geometry.
   int tile_y = 0, seg_x = 0, threads = 0, steps_per_pass = 1;
   int kernel = 1;   // 1 register-marching, 2 bulk-copy streamed, 3 lean streamed
+  int esz = 4;      // bytes per stored state value (4 FP32, 2 binary16)
   int stages = 0;   // streamed ring depth
   size_t smem = 0;  // dynamic shared memory per CTA
   // Two-step kernel (steps_per_pass == 2): CTA size, ring depths (ring A in
@@ -160,6 +161,8 @@ int32_t validate(const pjzfdtd_problem& p) {
     return fail(PJZFDTD_ERR_INVALID, "launch params must be >= 0");
   if (p.steps_per_pass > 2)
     return fail(PJZFDTD_ERR_INVALID, "steps_per_pass must be 0 (auto), 1 or 2");
+  if (p.storage != PJZFDTD_STORAGE_F32 && p.storage != PJZFDTD_STORAGE_F16)
+    return fail(PJZFDTD_ERR_INVALID, "storage must be 0 (FP32) or 1 (binary16)");
   return PJZFDTD_OK;
 }
 
@@ -296,7 +299,7 @@ constexpr bool kLeanAuto = false;
 int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   const pjzfdtd_problem& p = pl->p;
   const int Z = p.zz, ty = pl->tile_y;
-  const bool shape = lean_kernel_ptr(Z, ty) != nullptr;
+  const bool shape = lean_kernel_ptr(Z, ty, p.storage) != nullptr;
   const bool ok = shape && pl->steps_per_pass == 1 && p.pml_lo % 4 == 0 &&
                   p.pml_hi % 4 == 0 && (required || pl->src_ring == 0);
   if (!ok) {
@@ -317,7 +320,9 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   pl->kernel = 3;
   pl->threads = warps * 32 + 32;
   pl->src_ring = pl->src_rows = 0;
-  pl->smem = StreamGeom(ty, Z, pl->P).bytes(pl->stages);
+  pl->smem = p.storage == PJZFDTD_STORAGE_F16
+                 ? LeanGeom<__half>(ty, Z, pl->P).bytes(pl->stages)
+                 : LeanGeom<float>(ty, Z, pl->P).bytes(pl->stages);
   return PJZFDTD_OK;
 }
 
@@ -331,7 +336,14 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   if (pl->p.kernel >= 2 && (Z % 4 != 0 || Z > zmax))
     return fail(PJZFDTD_ERR_INVALID,
                 "the streamed kernels need zz %% 4 == 0 and zz <= %d", zmax);
-  if (pl->p.kernel == 3) {
+  if (pl->p.storage == PJZFDTD_STORAGE_F16 && pl->p.kernel != 0 &&
+      pl->p.kernel != 3)
+    return fail(PJZFDTD_ERR_UNSUPPORTED,
+                "binary16 storage is served by the lean kernel (kernel 0 or 3)");
+  if (pl->p.kernel == 3 || pl->p.storage == PJZFDTD_STORAGE_F16) {
+    if (Z % 4 != 0 || Z > zmax)
+      return fail(PJZFDTD_ERR_UNSUPPORTED,
+                  "binary16 storage needs the lean kernel (zz %% 4 == 0)");
     if (pl->p.steps_per_pass == 2)
       return fail(PJZFDTD_ERR_UNSUPPORTED,
                   "the lean kernel advances one step per launch");
@@ -392,7 +404,8 @@ void set_boxes(pjzfdtd_plan* pl) {
 void layout(pjzfdtd_plan* pl) {
   const pjzfdtd_problem& p = pl->p;
   const size_t N = (size_t)pl->N;
-  pl->Pp = round4(pl->P);
+  // PML state rows are whole 16-byte units (4 FP32 or 8 binary16 values).
+  pl->Pp = pl->esz == 2 ? (pl->P + 7) / 8 * 8 : round4(pl->P);
   pl->Yp = round4(p.yy);
   set_boxes(pl);
   const size_t XYP = (size_t)p.xx * p.yy * std::max(pl->Pp, 1);
@@ -402,11 +415,12 @@ void layout(pjzfdtd_plan* pl) {
     o = align256(o + bytes);
     return at;
   };
-  pl->off_fa = take(6 * N * sizeof(float));
-  pl->off_fb = take(6 * N * sizeof(float));
-  pl->off_cb = take(3 * N * sizeof(float));
-  pl->off_pa = take(4 * XYP * sizeof(float));
-  pl->off_pb = take(4 * XYP * sizeof(float));
+  const size_t es = (size_t)pl->esz;
+  pl->off_fa = take(6 * N * es);
+  pl->off_fb = take(6 * N * es);
+  pl->off_cb = take(3 * N * es);
+  pl->off_pa = take(4 * XYP * es);
+  pl->off_pb = take(4 * XYP * es);
   pl->off_zc = take(6 * (size_t)p.zz * sizeof(float));
   const size_t comp = (p.out_mode == PJZFDTD_OUT_PHASORS ||
                        p.out_mode == PJZFDTD_OUT_GRADIENT) ? pl->out_floats : 0;
@@ -434,7 +448,7 @@ cudaError_t set_stream_smem(const pjzfdtd_plan* pl, bool sr) {
 }
 
 cudaError_t set_lean_smem(const pjzfdtd_plan* pl) {
-  return cudaFuncSetAttribute(lean_kernel_ptr(pl->p.zz, pl->tile_y),
+  return cudaFuncSetAttribute(lean_kernel_ptr(pl->p.zz, pl->tile_y, pl->p.storage),
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)pl->smem);
 }
@@ -467,7 +481,8 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   } else if (pl->kernel == 3) {
     CUDA_TRY(set_lean_smem(pl));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, lean_kernel_ptr(pl->p.zz, pl->tile_y), pl->threads, pl->smem));
+        &per_sm, lean_kernel_ptr(pl->p.zz, pl->tile_y, pl->p.storage), pl->threads,
+        pl->smem));
   } else if (pl->kernel == 2) {
     CUDA_TRY(set_stream_smem(pl, pl->src_ring > 0));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
@@ -565,20 +580,32 @@ int32_t run_init(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   if (copy_zc)
     CUDA_TRY(cudaMemcpyAsync(w.zc, pl->zc.data(), pl->zc.size() * sizeof(float),
                              cudaMemcpyHostToDevice, st));
-  if (b->fields)
+  const bool f16 = pl->esz == 2;
+  const int threads = 256;
+  if (b->fields && f16) {
+    const long long n = 6 * N;
+    narrow_f16_kernel<<<(int)std::min<long long>((n + 255) / 256, 1 << 20), 256, 0,
+                        st>>>(b->fields, reinterpret_cast<__half*>(w.fa), n);
+    CUDA_TRY(cudaGetLastError());
+  } else if (b->fields) {
     CUDA_TRY(cudaMemcpyAsync(w.fa, b->fields, 6 * N * sizeof(float),
                              cudaMemcpyDeviceToDevice, st));
-  else
-    CUDA_TRY(cudaMemsetAsync(w.fa, 0, 6 * N * sizeof(float), st));
-  CUDA_TRY(cudaMemsetAsync(w.pa, 0, 4 * XYP * sizeof(float), st));
-  CUDA_TRY(cudaMemsetAsync(w.pb, 0, 4 * XYP * sizeof(float), st));
+  } else {
+    CUDA_TRY(cudaMemsetAsync(w.fa, 0, 6 * N * pl->esz, st));
+  }
+  CUDA_TRY(cudaMemsetAsync(w.pa, 0, 4 * XYP * pl->esz, st));
+  CUDA_TRY(cudaMemsetAsync(w.pb, 0, 4 * XYP * pl->esz, st));
   CUDA_TRY(cudaMemsetAsync(w.status, 0, sizeof(int), st));
-  const int threads = 256;
   const long long total = 3 * N;
   const int blocks = (int)std::min<long long>((total + threads - 1) / threads, 1 << 20);
-  precompute_cb_kernel<<<blocks, threads, 0, st>>>(
-      b->epsilon, b->absorption_mask, w.cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
-      p.rx, p.ry, p.rz, p.dt);
+  if (f16)
+    precompute_cb_kernel<__half><<<blocks, threads, 0, st>>>(
+        b->epsilon, b->absorption_mask, reinterpret_cast<__half*>(w.cb), p.xx,
+        p.yy, p.zz, p.ox, p.oy, p.oz, p.rx, p.ry, p.rz, p.dt);
+  else
+    precompute_cb_kernel<float><<<blocks, threads, 0, st>>>(
+        b->epsilon, b->absorption_mask, w.cb, p.xx, p.yy, p.zz, p.ox, p.oy, p.oz,
+        p.rx, p.ry, p.rz, p.dt);
   CUDA_TRY(cudaGetLastError());
   if (pl->kernel >= 2) {
     const long long nm = (long long)p.xx * 3 * pl->Yp;
@@ -687,15 +714,19 @@ int32_t record_step(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
     ra.comp = w.comp + pl->box_off[k];
     ra.comp_h = w.comph + pl->box_off[k];
     const int rblocks = (int)std::min<long long>((nb + 255) / 256, 1 << 20);
+    const bool f16 = pl->esz == 2;
     switch (p.out_mode) {
       case PJZFDTD_OUT_SNAPSHOTS:
-        record_kernel<kRecSnap><<<rblocks, 256, 0, st>>>(ra);
+        if (f16) record_kernel<kRecSnap, __half><<<rblocks, 256, 0, st>>>(ra);
+        else record_kernel<kRecSnap, float><<<rblocks, 256, 0, st>>>(ra);
         break;
       case PJZFDTD_OUT_PHASORS:
-        record_kernel<kRecProj><<<rblocks, 256, 0, st>>>(ra);
+        if (f16) record_kernel<kRecProj, __half><<<rblocks, 256, 0, st>>>(ra);
+        else record_kernel<kRecProj, float><<<rblocks, 256, 0, st>>>(ra);
         break;
       default:
-        record_kernel<kRecGrad><<<rblocks, 256, 0, st>>>(ra);
+        if (f16) record_kernel<kRecGrad, __half><<<rblocks, 256, 0, st>>>(ra);
+        else record_kernel<kRecGrad, float><<<rblocks, 256, 0, st>>>(ra);
         break;
     }
     CUDA_TRY(cudaGetLastError());
@@ -708,6 +739,13 @@ int32_t run_finish(const pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   if (!b->fields) return PJZFDTD_OK;
   RunPtrs w(pl, ws);
   float* fin = cur == 0 ? w.fa : w.fb;
+  if (pl->esz == 2) {
+    const long long n = 6 * pl->N;
+    widen_f16_kernel<<<(int)std::min<long long>((n + 255) / 256, 1 << 20), 256, 0,
+                       st>>>(reinterpret_cast<const __half*>(fin), b->fields, n);
+    CUDA_TRY(cudaGetLastError());
+    return PJZFDTD_OK;
+  }
   CUDA_TRY(cudaMemcpyAsync(b->fields, fin, 6 * pl->N * sizeof(float),
                            cudaMemcpyDeviceToDevice, st));
   return PJZFDTD_OK;
@@ -748,7 +786,7 @@ int32_t run_range(pjzfdtd_plan* pl, const pjzfdtd_buffers* b, void* ws,
   StreamKernel sk = nullptr, sk2 = nullptr;
   if (pl->kernel == 3) {
     CUDA_TRY(set_lean_smem(pl));
-    sk = lean_kernel_ptr(p.zz, pl->tile_y);
+    sk = lean_kernel_ptr(p.zz, pl->tile_y, p.storage);
   } else if (pl->kernel == 2) {
     // Ring-carried source rows need an aligned source profile (fixed per run).
     const bool sr = stream_args(pl, ws, step_args(pl, b, ws, n0, pl->cur)).src_tma;
@@ -880,6 +918,7 @@ int32_t pjzfdtd_plan_create(const pjzfdtd_problem* problem,
   pl->p = *problem;
   const pjzfdtd_problem& p = pl->p;
   pl->N = (long long)p.xx * p.yy * p.zz;
+  pl->esz = p.storage == PJZFDTD_STORAGE_F16 ? 2 : 4;
   pl->P = p.pml_lo + p.pml_hi;
   pl->ns = (p.out_mode != PJZFDTD_OUT_NONE && p.out_stop > p.out_start)
                ? (p.out_stop - p.out_start + p.out_step - 1) / p.out_step
@@ -1033,6 +1072,11 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
   size_t o = 0;
   for (int i = 0; i < n; ++i) {
     pjzfdtd_plan* pl = plans[i];
+    if (pl && pl->esz != 4) {
+      delete bt;
+      return fail(PJZFDTD_ERR_UNSUPPORTED,
+                  "plan %d stores binary16; batches run FP32 storage only", i);
+    }
     if (!pl || pl->kernel < 2) {
       delete bt;
       return fail(PJZFDTD_ERR_UNSUPPORTED,

@@ -7,6 +7,7 @@
 // Per element the operations are those of the CPU oracle, in its order.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include "step_kernel.cuh"
@@ -14,7 +15,7 @@
 namespace pjzfdtd {
 
 struct RecordArgs {
-  const float* __restrict__ f;  // [6][N] state after the step
+  const void* __restrict__ f;   // [6][N] state after the step (storage type)
   long long N;
   int X, Y, Z;
   int bx0, by0, bz0, bnx, bny, bnz;  // recorded box (region or gradient box)
@@ -28,8 +29,14 @@ struct RecordArgs {
   float w[kMaxRows];
 };
 
-template <int REC>
+__device__ __forceinline__ float widen(float v) { return v; }
+__device__ __forceinline__ float widen(__half v) { return __half2float(v); }
+
+// T: storage type of the state (float, or __half for reduced-precision
+// storage; the records and accumulators are FP32 either way).
+template <int REC, typename T>
 __global__ void record_kernel(const RecordArgs a) {
+  const T* f = static_cast<const T*>(a.f);
   const long long B = (long long)a.bnx * a.bny * a.bnz;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < B;
        t += (long long)gridDim.x * blockDim.x) {
@@ -41,12 +48,12 @@ __global__ void record_kernel(const RecordArgs a) {
         ((long long)(bx + a.bx0) * a.Y + (by + a.by0)) * a.Z + (bz + a.bz0);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      const float e = a.f[c * a.N + i];
+      const float e = widen(f[c * a.N + i]);
       if (REC == kRecSnap) {
         a.out[c * B + t] = e;
-        if (a.record_h) a.out_h[c * B + t] = a.f[(3 + c) * a.N + i];
+        if (a.record_h) a.out_h[c * B + t] = widen(f[(3 + c) * a.N + i]);
       } else if (REC == kRecProj) {
-        const float h = a.record_h ? a.f[(3 + c) * a.N + i] : 0.f;
+        const float h = a.record_h ? widen(f[(3 + c) * a.N + i]) : 0.f;
         for (int r = 0; r < a.rows; ++r) {
           const long long ai = ((long long)r * 3 + c) * B + t;
           kahan(&a.out[ai], &a.comp[ai], a.w[r], e);

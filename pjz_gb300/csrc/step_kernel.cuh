@@ -22,6 +22,7 @@
 // bit-identical to it.
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -239,10 +240,17 @@ __global__ void __launch_bounds__(kMaxThreads)
   }
 }
 
-// cb[c][x][y][z] = dt / (eps_c(clamped region index) + sigma_c(x,y) * dt/2).
+__device__ __forceinline__ void store_as(float* p, float v) { *p = v; }
+__device__ __forceinline__ void store_as(__half* p, float v) {
+  *p = __float2half_rn(v);
+}
+
+// cb[c][x][y][z] = dt / (eps_c(clamped region index) + sigma_c(x,y) * dt/2),
+// computed in FP32 and stored as T (rounded to nearest even for __half).
+template <typename T>
 __global__ void precompute_cb_kernel(const float* __restrict__ eps,
                                      const float* __restrict__ mask,
-                                     float* __restrict__ cb, int X, int Y, int Z,
+                                     T* __restrict__ cb, int X, int Y, int Z,
                                      int ox, int oy, int oz, int rx, int ry,
                                      int rz, float dt) {
   const long long N = (long long)X * Y * Z;
@@ -260,8 +268,23 @@ __global__ void precompute_cb_kernel(const float* __restrict__ eps,
     const int ez = min(max(z - oz, 0), rz - 1);
     const float e = eps[(((long long)c * rx + ex) * ry + ey) * rz + ez];
     const float s = mask[((long long)c * X + x) * Y + y];
-    cb[t] = __fdiv_rn(dt, __fmaf_rn(s, hdt, e));
+    store_as(&cb[t], __fdiv_rn(dt, __fmaf_rn(s, hdt, e)));
   }
+}
+
+// FP32 state in and out of binary16 storage (round to nearest even; the
+// widening is exact).
+__global__ void narrow_f16_kernel(const float* __restrict__ src,
+                                  __half* __restrict__ dst, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = __float2half_rn(src[t]);
+}
+__global__ void widen_f16_kernel(const __half* __restrict__ src,
+                                 float* __restrict__ dst, long long n) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = __half2float(src[t]);
 }
 
 #endif  // PJZ_HOST_KERNELS

@@ -21,6 +21,8 @@ OUT_NONE = _lib.OUT_NONE
 OUT_SNAPSHOTS = _lib.OUT_SNAPSHOTS
 OUT_PHASORS = _lib.OUT_PHASORS
 OUT_GRADIENT = _lib.OUT_GRADIENT
+STORAGE_F32 = _lib.STORAGE_F32
+STORAGE_F16 = _lib.STORAGE_F16
 
 
 def _f32_host(a) -> np.ndarray:
@@ -60,7 +62,8 @@ class Plan:
                grad_shape: Tuple[int, int, int] = (0, 0, 0),
                tile_y: int = 0, seg_x: int = 0, steps_per_pass: int = 0,
                kernel: int = 0, stages: int = 0, monitors=None, warps: int = 0,
-               wait_limit_kcycles: int = 0, test_stall_bytes: int = 0):
+               wait_limit_kcycles: int = 0, test_stall_bytes: int = 0,
+               storage: int = STORAGE_F32):
     lib = _lib.load()
     p = _lib.Problem()
     p.xx, p.yy, p.zz = (int(v) for v in domain)
@@ -81,6 +84,7 @@ class Plan:
     p.kernel, p.stages, p.warps = int(kernel), int(stages), int(warps)
     p.wait_limit_kcycles = int(wait_limit_kcycles)
     p.test_stall_bytes = int(test_stall_bytes)
+    p.storage = int(storage)
     zz = p.zz
     kap, sig, alp = (_f32_host(a) for a in (pml_kappa, pml_sigma, pml_alpha))
     for name, a in (("pml_kappa", kap), ("pml_sigma", sig), ("pml_alpha", alp)):
@@ -331,6 +335,15 @@ def plane_source_box(source_field: torch.Tensor, source_position: int,
   origin = [0, 0, 0]
   origin[axis] = lo
   return tuple(origin), tuple(shape), prof
+
+
+def run_many(plans, inputs):
+  """Runs independent plans: as one :class:`Batch` (one launch per time step
+  for all of them) when every plan stores FP32, else one after another
+  (batches run FP32 storage only).  Returns the ``(out, out_h)`` pairs."""
+  if all(p.problem.storage == STORAGE_F32 for p in plans):
+    return Batch(plans).run(inputs, graph=False)
+  return [p.run(**kw) for p, kw in zip(plans, inputs)]
 
 
 class Batch:

@@ -41,7 +41,7 @@ def oracle_kwargs(case):
           if k not in ("source_field", "source_position", "domain")}
 
 
-def field_oracle(wl, precision="f32", nthreads=0):
+def field_oracle(wl, precision="f32", nthreads=0, storage="f32"):
   """pjz's ``field`` of workload ``wl`` on the CPU oracle: the restated
   pre-processing (``oracle/pjz_ref.py``), the C Yee update in FP32 or FP64
   and the pinv projection accumulated at the sample steps; returns the
@@ -61,6 +61,6 @@ def field_oracle(wl, precision="f32", nthreads=0):
                  source_origin=org, source_profile=prof,
                  waveform=kw["source_waveform"], output_steps=kw["output_steps"],
                  mode="project", weights=w, precision=precision,
-                 nthreads=nthreads)["out"]
+                 nthreads=nthreads, storage=storage)["out"]
   ww = omega.shape[0]
   return r[:ww] + 1j * r[ww:]

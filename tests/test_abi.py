@@ -40,12 +40,12 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-  assert lib.pjzfdtd_abi_version() == 1
+  assert lib.pjzfdtd_abi_version() == 2
 
 
 def test_struct_sizes_match_header():
-  # 12 ints + float + 27 ints = 40 x 4 bytes.
-  assert ctypes.sizeof(_lib.Problem) == 160
+  # 12 ints + float + 28 ints = 41 x 4 bytes.
+  assert ctypes.sizeof(_lib.Problem) == 164
   assert ctypes.sizeof(_lib.Buffers) == 8 * 8
 
 
@@ -144,3 +144,41 @@ def test_lean_kernel_plans_resolve(lib, Z, pml):
   with pytest.raises(NotImplementedError, match="lean"):
     engine.Plan(**dict(kw, pml_widths=(3, 5), pml_kappa=np.ones((Z, 2)),
                        pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2))))
+
+
+@pytest.mark.parametrize("Z,pml,ok", [(64, (8, 8), True), (48, (4, 4), True),
+                                      (32, (8, 8), True), (64, (3, 5), False),
+                                      (40, (8, 8), False), (18, (3, 2), False)])
+def test_binary16_storage_plans(lib, Z, pml, ok):
+  """storage=1 (binary16) resolves to the lean kernel where it applies and
+  is refused elsewhere; its workspace holds 2-byte fields, coefficients and
+  z-PML state (state rows padded to 8 values)."""
+  Y = 33 if Z != 32 else 61
+  kw = dict(domain=(20, Y, Z), offset=(2, 2, 2), region=(16, Y - 4, Z - 4),
+            tt=50, dt=0.5, pml_widths=pml, pml_kappa=np.ones((Z, 2)),
+            pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)),
+            source_origin=(4, 0, 0), source_shape=(2, Y, Z), source_ncols=2,
+            output_steps=(30, 50, 5), out_mode=engine.OUT_SNAPSHOTS)
+  if not ok:
+    with pytest.raises(NotImplementedError):
+      engine.Plan(**kw, storage=engine.STORAGE_F16)
+    return
+  half = engine.Plan(**kw, storage=engine.STORAGE_F16)
+  full = engine.Plan(**kw)
+  assert half.launch_config()["kernel"] == 3
+  N = 20 * Y * Z
+  # 15 N stored values (two states of 6, 3 coefficients) per plan.
+  assert full.workspace_bytes - half.workspace_bytes >= 15 * N * 2 - 4096
+  with pytest.raises(NotImplementedError, match="lean"):
+    engine.Plan(**kw, storage=engine.STORAGE_F16, kernel=2)
+  with pytest.raises(ValueError, match="storage"):
+    engine.Plan(**kw, storage=2)
+
+
+def test_binary16_plans_stay_out_of_batches(lib):
+  Z = 64
+  kw = dict(domain=(20, 33, Z), offset=(0, 0, 0), region=(20, 33, Z), tt=20,
+            dt=0.5, pml_widths=(8, 8), pml_kappa=np.ones((Z, 2)),
+            pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)))
+  with pytest.raises(NotImplementedError, match="binary16"):
+    engine.Batch([engine.Plan(**kw, storage=engine.STORAGE_F16)])

@@ -26,7 +26,7 @@ def dev(a):
 
 def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
             tile_y=0, seg_x=0, fields=None, split=None, kernel=0, stages=0,
-            steps_per_pass=0):
+            steps_per_pass=0, storage=engine.STORAGE_F32):
   p = engine.Plan(domain=case["domain"], offset=case["offset"],
                   region=case["eps"].shape[1:], tt=case["tt"], dt=case["dt"],
                   pml_widths=case["pml_widths"], pml_kappa=case["kappa"],
@@ -37,7 +37,7 @@ def gpu_run(case, out_mode=engine.OUT_SNAPSHOTS, weights=None, record_h=False,
                   output_steps=case["output_steps"], out_mode=out_mode,
                   weights=weights, record_h=record_h, tile_y=tile_y,
                   seg_x=seg_x, kernel=kernel, stages=stages,
-                  steps_per_pass=steps_per_pass)
+                  steps_per_pass=steps_per_pass, storage=storage)
   if steps_per_pass:
     assert p.launch_config()["steps_per_pass"] == steps_per_pass
   args = dict(epsilon=dev(case["eps"]), absorption_mask=dev(case["mask"]),

@@ -7,7 +7,9 @@
   Kahan-compensated projection), and stay within 1e-5 relative L2 of the
   FP64 oracle over all five frequencies and three components (the field
   gate of the forward solve).  Both oracle legs run the C restatement on
-  every host core; their times are printed.
+  every host core; their times are printed.  The same solve with binary16
+  storage (use_reduced_precision=True) is held to 2e-2 of the FP64 oracle
+  and its error printed.
 * c3 shapes in one graph-captured batch: several of c3's uneven problems
   (x, y in {256, 384, 512}, z in {32, 48, 64}, 1-3 frequencies, their own
   designs and source planes) for 240 steps each, every problem's phasors
@@ -73,8 +75,14 @@ def test_c1_full_length_vs_fp32_and_fp64_oracle(native):
         f"(incl. set-up and copies), FP32 oracle {t32:.1f} s, FP64 oracle "
         f"{t64:.1f} s; bit-exact to FP32 oracle: {same}; rel-L2 vs FP64 "
         f"{err:.3e} (per frequency {', '.join(f'{e:.2e}' for e in per_freq)})")
+  sp16 = wl.sim_params._replace(use_reduced_precision=True)
+  got16 = pjz_gb300.field(dev(wl.epsilon), dev(wl.source), wl.omega,
+                          wl.source_pos, sp16).cpu().numpy()
+  err16 = np.linalg.norm(got16 - want64) / np.linalg.norm(want64)
+  print(f"c1 full length with binary16 storage: rel-L2 vs FP64 {err16:.3e}")
   assert same, np.abs(got - want32).max()
   assert err < 1e-5, err
+  assert err16 < 2e-2, err16
 
 
 def test_c3_shapes_batched_vs_oracle(native):

@@ -310,3 +310,19 @@ def test_c_oracle_matches_numpy_fp64_variants(orient, pml, kinf, full_region):
   assert scale > 0 and np.abs(snaps).max() > 0
   np.testing.assert_allclose(c["out"], snaps, rtol=0, atol=1e-12 * scale)
   np.testing.assert_allclose(c["fields"], fields, rtol=0, atol=1e-12 * scale)
+
+
+def test_oracle_binary16_rounding_matches_ieee():
+  """The oracle's reduced-precision storage rounds to IEEE binary16 with
+  round-to-nearest-even, subnormals and overflow to infinity, exactly as
+  numpy's float16 conversion does (and as the GPU's cvt.rn.f16.f32)."""
+  rng = np.random.default_rng(0)
+  vals = (rng.normal(size=4000) * 10.0 ** rng.integers(-9, 6, 4000)).astype(np.float32)
+  edge = np.float32([6.1e-5, 5.96e-8, 2.98e-8, 2.99e-8, 65504, 65519, 65520, 1e6,
+                     -0.0, 0.0, np.inf, -np.inf, 1 + 2 ** -11, 1 + 3 * 2 ** -11])
+  vals = np.concatenate([vals, edge])
+  got = np.array([oracle.round_f16(v) for v in vals], np.float32)
+  with np.errstate(over="ignore"):
+    want = vals.astype(np.float16).astype(np.float32)
+  assert np.array_equal(got, want)
+  assert np.array_equal(np.signbit(got), np.signbit(want))

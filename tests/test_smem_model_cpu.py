@@ -354,7 +354,7 @@ def lean_e(sm, it, Z, Pp, y0, RH, TY, hcur, hprev, RHZ, x, ring_e, Cs, c_lo, Ms,
 
 
 def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
-                 plant=None, hbuf=2, barriers=2, lean=False):
+                 plant=None, hbuf=2, barriers=2, lean=False, esz=4):
   """Replays CTA (tile, seg) of yee_stream_kernel; returns its Smem or None
   when the host refuses the tile.  `cover[x, y]` counts the rows stored.
   `plant` puts a known mistake into the replay (for the tests that show the
@@ -366,7 +366,8 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   stores of plane x are checked both right after its E phase and at the
   latest moment they may read, just before plane x + 2's wait on them."""
   P = plo + phi
-  Pp = r4(P)
+  # PML state rows are whole 16-byte units: 4 FP32 or 8 binary16 values.
+  Pp = r4(P) if esz == 4 else (P + 7) // 8 * 8
   Yp = r4(Y)
   RE, RH, MT = TY + 2, TY + 1, r4(TY) + 8
   e_off = 0
@@ -781,10 +782,10 @@ def run_grid(cta, X, Y, TY, seg_x, cover_shape):
 
 
 def one_step(X, Y, Z, plo, phi, TY, S, seg_x, ncomp, src, plant=None, hbuf=2,
-             barriers=2, lean=False):
+             barriers=2, lean=False, esz=4):
   def cta(tile, seg, cover):
     return one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src,
-                        cover, plant, hbuf, barriers, lean)
+                        cover, plant, hbuf, barriers, lean, esz)
   return run_grid(cta, X, Y, TY, seg_x, (X, Y))
 
 
@@ -951,18 +952,21 @@ LEAN_CASES = [(5, 30, 64, 14), (4, 41, 48, 19), (3, 61, 32, 29), (6, 9, 16, 5),
               (4, 13, 24, 3)]
 
 
+@pytest.mark.parametrize("esz", [4, 2])
 @pytest.mark.parametrize("X,Y,Z,TY", LEAN_CASES)
 @pytest.mark.parametrize("plo,phi", [(0, 0), (4, 4), (8, 8), (4, 8), (12, 4)])
-def test_lean_compute_accesses(X, Y, Z, TY, plo, phi):
+def test_lean_compute_accesses(X, Y, Z, TY, plo, phi, esz):
   """The lean kernel's items (z-quads, interior and PML warps) over ring
   depths and segments, with a tile boundary inside the domain and a ragged
-  last tile: in bounds, 16-byte aligned, reading exactly the data each
-  update needs, race-free between barriers, every row stored once."""
+  last tile: in bounds, quad-aligned (16 bytes for FP32, 8 for binary16
+  storage, whose PML state rows are 8 values), reading exactly the data
+  each update needs, race-free between barriers, every row stored once."""
   if plo + phi > Z:
     pytest.skip("slabs wider than the domain")
   checked = 0
   for S, seg_x in itertools.product((2, 3, 4), (2, X)):
-    res = one_step(X, Y, Z, plo, phi, TY, S, seg_x, min_ncomp(Z), None, lean=True)
+    res = one_step(X, Y, Z, plo, phi, TY, S, seg_x, min_ncomp(Z), None, lean=True,
+                   esz=esz)
     if res is None:
       continue
     reads, bad, cover = res
@@ -997,3 +1001,43 @@ def test_lean_model_flags_a_planted_mistake():
   assert one_step(*args, lean=True)[1] == []
   res = one_step(*args, plant="moff", lean=True)
   assert any(b[2] == "LE:mask" and b[3] == "stale" for b in res[1])
+
+
+def lean_geom(TY, Z, P, esz):
+  """Byte layout of a lean CTA (``LeanGeom`` in csrc/lean_kernel.cuh): slot
+  regions E, H, coefficients (stored type), absorber (FP32), PML state
+  (stored type, rows of Pp values); then new H, new E, new PML state."""
+  per16 = 16 // esz
+  Pp = (P + per16 - 1) // per16 * per16
+  RE, RH, MT = TY + 2, TY + 1, r4(TY) + 8
+  e = 0
+  h = e + 3 * RE * Z * esz
+  c = h + 3 * RH * Z * esz
+  m = c + 3 * TY * Z * esz
+  p = m + 3 * MT * 4
+  stage = p + 4 * RH * Pp * esz
+  return dict(Pp=Pp, e=e, h=h, c=c, m=m, p=p, stage=stage,
+              hn=2 * 3 * RH * Z * esz, en=2 * 3 * TY * Z * esz,
+              pn=2 * 4 * TY * Pp * esz)
+
+
+@pytest.mark.parametrize("esz", [4, 2])
+@pytest.mark.parametrize("Z,TY", [(64, 14), (48, 19), (32, 29), (32, 28)])
+@pytest.mark.parametrize("P", [0, 8, 12, 16, 24])
+def test_lean_geometry_bulk_copy_alignment(esz, Z, TY, P):
+  """Every region a bulk copy fills or drains starts on a 16-byte boundary
+  and every copied row (E/H/coefficient rows of Z values, PML state rows of
+  Pp values, whole absorber windows) is a whole number of 16-byte units,
+  for FP32 and binary16 storage; FP32 is the streamed kernel's layout."""
+  g = lean_geom(TY, Z, P, esz)
+  for k in ("e", "h", "c", "m", "p", "stage", "hn", "en", "pn"):
+    assert g[k] % 16 == 0, (k, g[k])
+  assert (Z * esz) % 16 == 0 and (g["Pp"] * esz) % 16 == 0
+  assert g["Pp"] >= P and g["Pp"] - P < 16 // esz
+  if esz == 4:
+    RE, RH, MT = TY + 2, TY + 1, r4(TY) + 8
+    stage = 3 * RE * Z + 3 * RH * Z + 3 * TY * Z + 3 * MT + 4 * RH * r4(P)
+    assert g["stage"] == 4 * stage
+  # Quads (4 values) of every region are 16-byte (FP32) / 8-byte (binary16)
+  # aligned: region starts are 16-byte aligned and rows hold whole quads.
+  assert Z % 4 == 0 and g["Pp"] % 4 == 0
