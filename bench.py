@@ -65,7 +65,7 @@ def _args():
   ap.add_argument("--no-f16", action="store_true",
                   help="c1: skip the binary16-storage leg")
   ap.add_argument("--kernel", type=int, default=0,
-                  help="0 auto, 1 register-marching, 2 streamed")
+                  help="0 auto, 1 register-marching, 2 streamed, 3 lean streamed")
   ap.add_argument("--stages", type=int, default=0)
   ap.add_argument("--tile-y", type=int, default=0)
   ap.add_argument("--seg-x", type=int, default=0)
@@ -326,8 +326,9 @@ def run_native(args):
   achieved = BYTES_PER_CELL * cells_per_launch / (launch_ms / 1e3) / 1e9
   effective = BYTES_PER_CELL * cells_per_launch * nl / launches / (launch_ms / 1e3) / 1e9
   peak, peak_kind = _peaks()
-  kname = ("yee_stream2" if cfg0["steps_per_pass"] == 2 else "yee_stream"
-           if cfg0["kernel"] == 2 else "yee_step")
+  kname = {(3, 2): "yee_lean2", (3, 1): "yee_lean", (2, 2): "yee_stream2",
+           (2, 1): "yee_stream"}.get((cfg0["kernel"], cfg0["steps_per_pass"]),
+                                     "yee_step")
   bpc, prof_d = _profile_traffic(f"{kname}_{args.workload}")
   roofline = {"bound": "hbm", "achieved": achieved, "peak": peak,
               "unit": "GB/s", "frac": achieved / peak,

@@ -30,6 +30,8 @@ inline BatchKernel batch_kernel_ptr(int steps) {
 // Lean single-step streamed kernel for (zz, tile_y) and storage (0 FP32,
 // 1 binary16) (kern_lean.cu), or nullptr when no compile-time shape matches.
 StreamKernel lean_kernel_ptr(int zz, int tile_y, int storage);
+// Lean two-step streamed kernel, likewise (kern_lean2.cu).
+StreamKernel lean2_kernel_ptr(int zz, int tile_y, int storage);
 // Block size bound of the lean kernel.
 constexpr int kLeanThreads = 384;
 // Permittivity rendering kernel (kern_render.cu).

@@ -24,6 +24,7 @@
 #include "stream_kernel.cuh"
 #include "stream2_kernel.cuh"
 #include "lean_kernel.cuh"
+#include "lean2_kernel.cuh"
 #include "record_kernel.cuh"
 #include "kernel_table.cuh"
 
@@ -300,8 +301,9 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   const pjzfdtd_problem& p = pl->p;
   const int Z = p.zz, ty = pl->tile_y;
   const bool shape = lean_kernel_ptr(Z, ty, p.storage) != nullptr;
-  const bool ok = shape && pl->steps_per_pass == 1 && p.pml_lo % 4 == 0 &&
-                  p.pml_hi % 4 == 0 && (required || pl->src_ring == 0);
+  const bool ok = shape && (required || pl->steps_per_pass == 1) &&
+                  p.pml_lo % 4 == 0 && p.pml_hi % 4 == 0 &&
+                  (required || pl->src_ring == 0);
   if (!ok) {
     if (!required) return PJZFDTD_OK;
     return fail(PJZFDTD_ERR_UNSUPPORTED,
@@ -326,6 +328,27 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   return PJZFDTD_OK;
 }
 
+// Lean two-step kernel (lean2_kernel.cuh) on a plan already resolved for
+// the lean one-step kernel with two steps per pass: its compile-time shape,
+// block and shared memory (the ring depths of the streamed two-step plan).
+int32_t resolve_lean2(pjzfdtd_plan* pl) {
+  const pjzfdtd_problem& p = pl->p;
+  const int Z = p.zz, ty = pl->tile_y;
+  if (!lean2_kernel_ptr(Z, ty, p.storage))
+    return fail(PJZFDTD_ERR_UNSUPPORTED,
+                "the lean two-step kernel needs (zz, tile_y) = (64, 14), got "
+                "(%d, %d)", Z, ty);
+  const int warps = lean2_warps(Z, ty, p.pml_lo, p.pml_hi);
+  if (warps * 32 + 32 > kLeanThreads)
+    return fail(PJZFDTD_ERR_UNSUPPORTED, "lean two-step tile needs %d warps", warps);
+  const int s2 = pl->stages2 & 0xff;
+  pl->threads2 = warps * 32 + 32;
+  pl->smem2 = p.storage == PJZFDTD_STORAGE_F16
+                  ? Lean2Geom<__half>(ty, Z, pl->P).bytes(s2, s2)
+                  : Lean2Geom<float>(ty, Z, pl->P).bytes(s2, s2);
+  return PJZFDTD_OK;
+}
+
 // Resolves the CTA tile.  Register-marching kernel: (tile_y + 2) * zz
 // cells, one thread each, at most kMaxThreads threads.
 int32_t resolve_tile(pjzfdtd_plan* pl) {
@@ -344,12 +367,10 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
     if (Z % 4 != 0 || Z > zmax)
       return fail(PJZFDTD_ERR_UNSUPPORTED,
                   "binary16 storage needs the lean kernel (zz %% 4 == 0)");
-    if (pl->p.steps_per_pass == 2)
-      return fail(PJZFDTD_ERR_UNSUPPORTED,
-                  "the lean kernel advances one step per launch");
     int32_t rc = resolve_stream(pl);
     if (rc) return rc;
-    return resolve_lean(pl, true);
+    if ((rc = resolve_lean(pl, true))) return rc;
+    return pl->steps_per_pass == 2 ? resolve_lean2(pl) : PJZFDTD_OK;
   }
   if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax)) {
     int32_t rc = resolve_stream(pl);
@@ -453,8 +474,10 @@ cudaError_t set_lean_smem(const pjzfdtd_plan* pl) {
                               (int)pl->smem);
 }
 
-// The two-step kernel for a plan, by the same rule.
+// The two-step kernel for a plan, by the same rule (the lean one for lean
+// plans).
 StreamKernel stream2_kernel_for(const pjzfdtd_plan* pl) {
+  if (pl->kernel == 3) return lean2_kernel_ptr(pl->p.zz, pl->tile_y, pl->p.storage);
   return stream2_kernel_ptr(pl->p.zz, pl->tile_y);
 }
 
@@ -474,7 +497,7 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   CUDA_TRY(cudaGetDevice(&dev));
   CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int per_sm = 1;
-  if (pl->kernel == 2 && pl->steps_per_pass == 2) {
+  if (pl->kernel >= 2 && pl->steps_per_pass == 2) {
     CUDA_TRY(set_stream2_smem(pl));
     CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
         &per_sm, stream2_kernel_for(pl), pl->threads2, pl->smem2));
@@ -1257,12 +1280,12 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
                 xx, yy, zz, magnification);
   if (ll > 1 && !interface_positions)
     return fail(PJZFDTD_ERR_INVALID, "%d interface positions needed", ll - 1);
-  const size_t smem = render_smem_floats(ll, zz) * sizeof(float);
+  const size_t smem = render_smem_floats(ll, zz, magnification) * sizeof(float);
   const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
   if (smem > kSmemMax || yblocks > 65535)
     return fail(PJZFDTD_ERR_INVALID,
-                "zz = %d with %d layers (or yy = %d) exceeds one CTA's reach",
-                zz, ll, yy);
+                "zz = %d with %d layers at magnification %d (or yy = %d) "
+                "exceeds one CTA's reach", zz, ll, magnification, yy);
   RenderArgs a = {};
   a.layers = layers;
   a.out = out;
@@ -1277,7 +1300,7 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   if (smem > 48 * 1024)
     CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-  const dim3 grid((unsigned)xx, 3, (unsigned)yblocks);
+  const dim3 grid((unsigned)xx, (unsigned)yblocks);
   k<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(a);
   CUDA_TRY(cudaGetLastError());
   return PJZFDTD_OK;

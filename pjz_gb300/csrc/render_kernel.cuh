@@ -18,20 +18,25 @@
 // mixed by the squared share of the component's axis in the slope vector
 // (subpixel smoothing, diagonal of the interface projection only).
 //
-// One CTA per (x, component, block of kRenderTileY y cells): it tabulates
-// the z occupancy of its component's cells and the window statistics of its
-// y cells in shared memory, then writes its (y, z) outputs with z fastest.
-// A z cell that lies wholly inside one layer (its fraction exactly 1, all
-// others exactly 0) has the same value at every such z of a column: it is
-// computed once per (y, layer) and copied, and only the cells an interface
-// cuts take the full mix.  Both give the same floats when every layer's
-// window statistics at that (x, y) are finite (the full mix then adds exact
-// zeros to that layer's terms); where one is not (a zero pixel makes the
-// mean of the inverse infinite, a NaN pixel makes everything NaN), 0 * inf
-// in the full mix gives NaN as pjz's einsum does, so such columns take the
-// full mix at every z.  FP32 throughout; the per-cell
-// functions are __host__ __device__ so that a host emulation of the block
-// loop checks the same code on the CPU.
+// One CTA per (x, block of kRenderTileY y cells), all three components.
+// It tabulates the z occupancy of each component's cells, then, one layer
+// at a time, stages the layer's pixel patch that the block's windows cover
+// (3m rows x (2m*ny + m) columns, edge pixels repeated) in shared memory
+// with each pixel's reciprocal computed once, computes every window's
+// statistics from the patch, and finally writes the (component, y, z)
+// outputs with z fastest, coalesced.  A z cell that lies wholly inside one
+// layer (its fraction exactly 1, all others exactly 0) has the same value at
+// every such z of a column: it is computed once per (y, layer) and copied,
+// and only the cells an interface cuts take the full mix.  Both give the
+// same floats when every layer's window statistics at that (x, y) are
+// finite (the full mix then adds exact zeros to that layer's terms); where
+// one is not (a zero pixel makes the mean of the inverse infinite, a NaN
+// pixel makes everything NaN), 0 * inf in the full mix gives NaN as pjz's
+// einsum does, so such columns take the full mix at every z.  FP32
+// throughout, the window sums in the order of the original per-window loop
+// (rows outer, columns inner); the per-cell functions are __host__
+// __device__ so that a host emulation of the block loop checks the same code
+// on the CPU.
 #pragma once
 
 #include <math.h>
@@ -76,13 +81,22 @@ PJZ_HD float render_load(const float* layer, size_t i) { return layer[i]; }
 
 PJZ_HD int render_imax(int a, int b) { return a > b ? a : b; }
 
-// Shared-memory floats of one CTA: occupancy [2][ll][zz], the layer that
-// fills each z cell [zz] (int, -1 when an interface cuts it), statistics
-// [kRenderTileY][ll] of 4 floats, one-layer values [kRenderTileY][ll], and
-// per y cell whether every layer's statistics are finite [kRenderTileY]
-// (int).
-PJZ_HD size_t render_smem_floats(int ll, int zz) {
-  return 2 * (size_t)ll * zz + zz + 5 * (size_t)kRenderTileY * ll + kRenderTileY;
+// Pixel patch of one CTA and layer: rows k*x - m .. k*x + 2m - 1 and
+// columns k*y0 - m .. k*(y0 + ny) - 1 (k = 2m), negative indices repeating
+// the edge pixel.
+PJZ_HD int render_patch_rows(int m) { return 3 * m; }
+PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
+
+// Shared-memory floats of one CTA: occupancy frac / mid [3][ll][zz], the
+// layer that fills each z cell [3][zz] (int, -1 when an interface cuts it),
+// window statistics [3][kRenderTileY][ll] of 4 floats, one-layer values
+// [3][kRenderTileY][ll], per (component, y) whether every layer's statistics
+// are finite [3][kRenderTileY] (int), the pixel patch and its reciprocals
+// [2][3m][2m*kRenderTileY + m], and the pixel offsets u [2m].
+PJZ_HD size_t render_smem_floats(int ll, int zz, int m) {
+  return 6 * (size_t)ll * zz + 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
+         3 * kRenderTileY +
+         2 * (size_t)render_patch_rows(m) * render_patch_cols(m) + 2 * m;
 }
 
 PJZ_HD bool render_finite(const WindowStats& w) {
@@ -101,25 +115,32 @@ PJZ_HD void render_occupancy(const RenderArgs& a, int c, int l, int z,
   *mid = 0.5f * (b + t) - 0.5f * (lo + hi);
 }
 
-// Statistics of layer `l` over the pixel window of component `c` at (x, y).
-PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int l, int x, int y) {
-  const int k = 2 * a.m;
-  const int PX = k * a.xx, PY = k * a.yy;
-  const int sx = c != 0 ? a.m : 0, sy = c != 1 ? a.m : 0;
-  const float* L = a.layers + (size_t)l * PX * PY;
+// Offset of pixel i of a window from the window centre, in cells.
+PJZ_HD float render_u(const RenderArgs& a, int i) {
   const float c0 = (float)a.m - 0.5f;
+  return ((float)i - c0) / (float)(2 * a.m);
+}
+
+// Statistics of one layer over the pixel window of component `c` at tile
+// row yl, from the staged patch `pf` (pixels) and `pinv` (their
+// reciprocals) with row stride `pc`; `u` holds render_u of 0 .. 2m-1.
+PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
+                                 const float* pf, const float* pinv, int pc,
+                                 const float* u) {
+  const int k = 2 * a.m;
+  const int ioff = c == 0 ? a.m : 0;           // rows shifted unless Ex
+  const int joff = k * yl + (c == 1 ? a.m : 0);  // columns shifted unless Ey
   float s = 0.f, si = 0.f, sxu = 0.f, syu = 0.f;
   for (int i = 0; i < k; ++i) {
-    const int px = render_imax(k * x + i - sx, 0);
-    const float ui = ((float)i - c0) / (float)k;
+    const float ui = u[i];
+    const float* rf = pf + (i + ioff) * pc + joff;
+    const float* ri = pinv + (i + ioff) * pc + joff;
     for (int j = 0; j < k; ++j) {
-      const int py = render_imax(k * y + j - sy, 0);
-      const float uj = ((float)j - c0) / (float)k;
-      const float f = render_load(L, (size_t)px * PY + py);
+      const float f = rf[j];
       s += f;
-      si += 1.0f / f;
+      si += ri[j];
       sxu += f * ui;
-      syu += f * uj;
+      syu += f * u[j];
     }
   }
   const float n = (float)(k * k);
@@ -129,6 +150,23 @@ PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int l, int x, int y
   w.gx = 12.0f * sxu / n;
   w.gy = 12.0f * syu / n;
   return w;
+}
+
+// Stages pixel `t` of the patch of layer `l` for the CTA at (x, y0) with
+// ny tile rows: the pixel and its reciprocal.  Columns past the block's
+// windows (a short last tile) are left alone.
+PJZ_HD void render_stage(const RenderArgs& a, int l, int x, int y0, int ny, int t,
+                         float* pf, float* pinv) {
+  const int k = 2 * a.m, pc = render_patch_cols(a.m);
+  const int r = t / pc, cc = t - r * pc;
+  if (cc >= k * ny + a.m) return;
+  const int PX = k * a.xx, PY = k * a.yy;
+  const int px = render_imax(k * x - a.m + r, 0);
+  const int py = render_imax(k * y0 - a.m + cc, 0);
+  const float* L = a.layers + (size_t)l * PX * PY;
+  const float f = render_load(L, (size_t)px * PY + py);
+  pf[t] = f;
+  pinv[t] = 1.0f / f;
 }
 
 // The value from the fraction-weighted sums over the layers.
@@ -177,36 +215,56 @@ PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) 
 }
 
 #if defined(__CUDACC__) && defined(PJZ_RENDER_KERNEL)  // kern_render.cu only
-// grid (xx, 3, ceil(yy / kRenderTileY)); dynamic shared memory
-// render_smem_floats(ll, zz) floats.
+// grid (xx, ceil(yy / kRenderTileY)); dynamic shared memory
+// render_smem_floats(ll, zz, m) floats.
 __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a) {
   extern __shared__ __align__(16) float rsm[];
-  const int x = blockIdx.x, c = blockIdx.y, y0 = blockIdx.z * kRenderTileY;
+  const int x = blockIdx.x, y0 = blockIdx.y * kRenderTileY;
   const int ny = min(kRenderTileY, a.yy - y0);
-  float* frac = rsm;
-  float* mid = frac + a.ll * a.zz;
-  int* owner = reinterpret_cast<int*>(mid + a.ll * a.zz);
-  WindowStats* st = reinterpret_cast<WindowStats*>(owner + a.zz);
-  float* ival = reinterpret_cast<float*>(st + kRenderTileY * a.ll);
-  int* yfin = reinterpret_cast<int*>(ival + kRenderTileY * a.ll);
-  for (int z = threadIdx.x; z < a.zz; z += blockDim.x) {
+  const int LZ = a.ll * a.zz, TL = kRenderTileY * a.ll;
+  float* frac = rsm;                                   // [3][ll][zz]
+  float* mid = frac + 3 * LZ;                          // [3][ll][zz]
+  int* owner = reinterpret_cast<int*>(mid + 3 * LZ);   // [3][zz]
+  WindowStats* st = reinterpret_cast<WindowStats*>(owner + 3 * a.zz);  // [3][TY][ll]
+  float* ival = reinterpret_cast<float*>(st + 3 * TL);  // [3][TY][ll]
+  int* yfin = reinterpret_cast<int*>(ival + 3 * TL);   // [3][TY]
+  float* pf = reinterpret_cast<float*>(yfin + 3 * kRenderTileY);
+  const int pc = render_patch_cols(a.m);
+  const int np = render_patch_rows(a.m) * pc;
+  float* pinv = pf + np;
+  float* u = pinv + np;                                // [2m]
+  for (int t = threadIdx.x; t < 3 * a.zz; t += blockDim.x) {
+    const int c = t / a.zz, z = t - c * a.zz;
     for (int l = 0; l < a.ll; ++l)
-      render_occupancy(a, c, l, z, &frac[l * a.zz + z], &mid[l * a.zz + z]);
-    owner[z] = render_owner(a, frac, z);
+      render_occupancy(a, c, l, z, &frac[c * LZ + l * a.zz + z],
+                       &mid[c * LZ + l * a.zz + z]);
+    owner[t] = render_owner(a, frac + c * LZ, z);
   }
-  if (threadIdx.x < kRenderTileY) yfin[threadIdx.x] = 1;
-  __syncthreads();
-  for (int i = threadIdx.x; i < ny * a.ll; i += blockDim.x) {
-    st[i] = render_window(a, c, i % a.ll, x, y0 + i / a.ll);
-    ival[i] = render_interior(a, c, st[i]);
-    if (!render_finite(st[i])) yfin[i / a.ll] = 0;  // every writer stores 0
+  for (int t = threadIdx.x; t < 3 * kRenderTileY; t += blockDim.x) yfin[t] = 1;
+  for (int t = threadIdx.x; t < 2 * a.m; t += blockDim.x) u[t] = render_u(a, t);
+  for (int l = 0; l < a.ll; ++l) {
+    __syncthreads();  // the previous layer's windows are done with the patch
+    for (int t = threadIdx.x; t < np; t += blockDim.x)
+      render_stage(a, l, x, y0, ny, t, pf, pinv);
+    __syncthreads();
+    for (int t = threadIdx.x; t < 3 * ny; t += blockDim.x) {
+      const int c = t / ny, yl = t - c * ny;
+      const int i = (c * kRenderTileY + yl) * a.ll + l;
+      st[i] = render_window(a, c, yl, pf, pinv, pc, u);
+      ival[i] = render_interior(a, c, st[i]);
+      if (!render_finite(st[i])) yfin[c * kRenderTileY + yl] = 0;  // all store 0
+    }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < ny * a.zz; i += blockDim.x) {
-    const int yl = i / a.zz, z = i - yl * a.zz;
-    const int o = yfin[yl] ? owner[z] : -1;
+  for (int t = threadIdx.x; t < 3 * ny * a.zz; t += blockDim.x) {
+    const int c = t / (ny * a.zz);
+    const int r = t - c * ny * a.zz;
+    const int yl = r / a.zz, z = r - yl * a.zz;
+    const int cy = c * kRenderTileY + yl;
+    const int o = yfin[cy] ? owner[c * a.zz + z] : -1;
     a.out[render_out_index(a, c, x, y0 + yl, z)] =
-        o >= 0 ? ival[yl * a.ll + o] : render_value(a, c, st + yl * a.ll, frac, mid, z);
+        o >= 0 ? ival[cy * a.ll + o]
+               : render_value(a, c, st + cy * a.ll, frac + c * LZ, mid + c * LZ, z);
   }
 }
 #endif

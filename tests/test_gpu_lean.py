@@ -87,3 +87,74 @@ def test_lean_c1_domain_short_run_bit_exact(native):
   want = oracle.run(**oracle_kwargs(case))["out"]
   got, _, _ = gpu_run(case, kernel=3)
   assert np.array_equal(got, want)
+
+
+# ---- lean two-step kernel (kernel=3, steps_per_pass=2) ----
+
+STORES = [(engine.STORAGE_F32, "f32"), (engine.STORAGE_F16, "f16")]
+
+
+@pytest.mark.parametrize("storage,ostore", STORES, ids=["f32", "f16"])
+@pytest.mark.parametrize("pml", [(8, 8), (4, 4), (0, 0), (4, 12)])
+@pytest.mark.parametrize("src", ["x", "y", "z"])
+def test_lean2_snapshots_bit_exact(native, storage, ostore, pml, src):
+  """Two steps per launch with the lean compute path, a tile boundary and
+  segment boundaries inside the domain: bit-identical to the oracle (FP32,
+  or binary16 storage)."""
+  case = random_problem(hash((pml, src, 2)) % 1000, X=19, Y=33, Z=64, pml=pml,
+                        src=src, src_pos=5 if src == "z" else 7, tt=25,
+                        steps=(9, 25, 4))
+  want = oracle.run(**oracle_kwargs(case), storage=ostore)["out"]
+  got, _, _ = gpu_run(case, kernel=3, steps_per_pass=2, seg_x=6, storage=storage)
+  assert np.array_equal(got, want), np.abs(got - want).max()
+
+
+@pytest.mark.parametrize("storage,ostore", STORES, ids=["f32", "f16"])
+@pytest.mark.parametrize("tt,steps", [(47, (5, 47, 3)), (40, (0, 40, 1)),
+                                      (41, (-6, 41, 2)), (9, (8, 9, 1))])
+def test_lean2_schedule_around_samples(native, storage, ostore, tt, steps):
+  """Two steps per launch except where a sampled state sits between them,
+  the sampled steps run by the lean one-step kernel: odd and even sample
+  steps, every step sampled, odd tt, samples before step 0; with recorded H
+  and final state."""
+  case = random_problem(61, X=15, Y=30, Z=64, pml=(8, 8), tt=tt, steps=steps)
+  f0 = np.random.default_rng(3).normal(size=(6,) + case["domain"]).astype(np.float32)
+  want = oracle.run(**oracle_kwargs(case), record_h=True, fields=f0.copy(),
+                    storage=ostore)
+  got, got_h, got_f = gpu_run(case, kernel=3, steps_per_pass=2, record_h=True,
+                              fields=f0.copy(), seg_x=4, storage=storage)
+  assert np.array_equal(got, want["out"])
+  assert np.array_equal(got_h, want["out_h"])
+  assert np.array_equal(got_f, want["fields"])
+
+
+@pytest.mark.parametrize("storage,ostore", STORES, ids=["f32", "f16"])
+def test_lean2_phasors_chaining_and_segments(native, storage, ostore):
+  case = random_problem(62, X=21, Y=31, Z=64, pml=(8, 8), tt=48, steps=(10, 48, 3))
+  ns = len(range(*case["output_steps"]))
+  w = np.random.default_rng(4).normal(size=(10, ns)).astype(np.float32)
+  want = oracle.run(**oracle_kwargs(case), mode="project", weights=w,
+                    storage=ostore)["out"]
+  for seg_x, split in ((1, None), (5, 23), (21, None)):
+    got, _, _ = gpu_run(case, out_mode=engine.OUT_PHASORS, weights=w, kernel=3,
+                        steps_per_pass=2, seg_x=seg_x, split=split,
+                        storage=storage)
+    assert np.array_equal(got, want), (seg_x, split)
+
+
+def test_lean2_c1_domain_short_run_bit_exact(native):
+  """The 512x512x64 c1 domain for 25 steps, two per launch."""
+  wl = workloads.design_c1(tt=25, ww=5)
+  sp = wl.sim_params
+  kw, omega = pjz_ref.field_setup(wl.epsilon, wl.source, wl.omega, wl.source_pos,
+                                  pjz_ref.SimParams(*sp[:-1]), zz=wl.domain[2])
+  org, shp, prof = oracle.plane_source_box(kw["source_field"],
+                                           kw["source_position"], wl.domain)
+  case = dict(eps=kw["epsilon"], offset=kw["offset"], mask=kw["absorption_mask"],
+              kappa=kw["pml_kappa"], sigma=kw["pml_sigma"], alpha=kw["pml_alpha"],
+              dt=0.5, tt=25, pml_widths=kw["pml_widths"], source_origin=org,
+              source_profile=prof, waveform=kw["source_waveform"],
+              output_steps=(10, 25, 4), domain=wl.domain)
+  want = oracle.run(**oracle_kwargs(case))["out"]
+  got, _, _ = gpu_run(case, kernel=3, steps_per_pass=2)
+  assert np.array_equal(got, want)

@@ -570,12 +570,76 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   return sm
 
 
-def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
+def h_quad(sm, ph, it, Z, Y, Pp, ras, ys, Ep, E1p, Ho, Pin):
+  """Shared-memory reads of lean H updates (quads): items ``it`` (thread,
+  quad start, PML column, PML warp) at buffer rows ``ras`` (domain rows
+  ``ys``): E rows ra and ra + 1 and z + 4, E of plane x + 1, old H, PML
+  state comps 0 and 1."""
+  thr, z0, col, pml = it
+  ie = ras * Z + z0
+  for c in range(3):
+    sm.read(ph + ":E", Ep.base + c * Ep.stride + ie, thr, Ep.T(c, ys), False,
+            Ep.lo, Ep.hi, 4)
+  up = ys + 1 >= Y
+  sm.read(ph + ":Ex y+1", Ep.base + ie + Z, thr, Ep.T(0, ys + 1), up, Ep.lo, Ep.hi, 4)
+  sm.read(ph + ":Ez y+1", Ep.base + 2 * Ep.stride + ie + Z, thr, Ep.T(2, ys + 1), up,
+          Ep.lo, Ep.hi, 4)
+  zin = z0 + 4 < Z
+  sm.read(ph + ":Ex z+1", (Ep.base + ie + 4)[zin], thr[zin], Ep.T(0, ys[zin]),
+          False, Ep.lo, Ep.hi)
+  sm.read(ph + ":Ey z+1", (Ep.base + Ep.stride + ie + 4)[zin], thr[zin],
+          Ep.T(1, ys[zin]), False, Ep.lo, Ep.hi)
+  if E1p is not None:
+    for c in (1, 2):
+      sm.read(ph + ":E x+1", E1p.base + c * E1p.stride + ie, thr, E1p.T(c, ys), False,
+              E1p.lo, E1p.hi, 4)
+  for c in range(3):
+    sm.read(ph + ":H", Ho.base + c * Ho.stride + ie, thr, Ho.T(c, ys), False, Ho.lo,
+            Ho.hi, 4)
+  pi = ras * Pp + col
+  for c in range(2):
+    sm.read(ph + ":psi", (Pin.base + c * Pin.stride + pi)[pml], thr[pml],
+            Pin.T(c, ys[pml]), False, Pin.lo, Pin.hi, 4)
+
+
+def e_quad(sm, ph, it, Z, Pp, ras, ys, Hx, Hy, Hz, Hyp, Hzp, prev0, Eo, Cb, Pin):
+  """Shared-memory reads of lean E updates (quads) at buffer rows ``ras``:
+  new H of the plane (rows ra, ra - 1, z - 1), new H y/z of plane x - 1
+  (zero when ``prev0``), old E, coefficients, PML state comps 2, 3."""
+  thr, z0, col, pml = it
+  ih = ras * Z + z0
+  for p in (Hx, Hy, Hz):
+    sm.read(ph + ":H", p.base + ih, thr, p.T(0, ys), False, p.lo, p.hi, 4)
+  down = ys - 1 < 0
+  sm.read(ph + ":Hx y-1", Hx.base + ih - Z, thr, Hx.T(0, ys - 1), down, Hx.lo,
+          Hx.hi, 4)
+  sm.read(ph + ":Hz y-1", Hz.base + ih - Z, thr, Hz.T(0, ys - 1), down, Hz.lo,
+          Hz.hi, 4)
+  zin = z0 > 0
+  sm.read(ph + ":Hx z-1", (Hx.base + ih - 1)[zin], thr[zin], Hx.T(0, ys[zin]),
+          False, Hx.lo, Hx.hi)
+  sm.read(ph + ":Hy z-1", (Hy.base + ih - 1)[zin], thr[zin], Hy.T(0, ys[zin]),
+          False, Hy.lo, Hy.hi)
+  for p in (Hyp, Hzp):
+    sm.read(ph + ":H x-1", p.base + ih, thr, p.T(0, ys), prev0, p.lo, p.hi, 4)
+  for c in range(3):
+    sm.read(ph + ":E", Eo.base + c * Eo.stride + ih, thr, Eo.T(c, ys), False, Eo.lo,
+            Eo.hi, 4)
+    sm.read(ph + ":cb", Cb.base + c * Cb.stride + ih, thr, Cb.T(c, ys), False, Cb.lo,
+            Cb.hi, 4)
+  pi = ras * Pp + col
+  for c in range(2):
+    sm.read(ph + ":psi", (Pin.base + c * Pin.stride + pi)[pml], thr[pml],
+            Pin.T(c, ys[pml]), False, Pin.lo, Pin.hi, 4)
+
+
+def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover,
+                 lean=False, esz=4):
   """Replays CTA (tile, seg) of yee_stream2_kernel; returns its Smem or None
   when the host refuses the tile.  Level-2 results go straight to global
   memory; `cover[level - 1 of the phase, x, y]` counts the rows stored."""
   P = plo + phi
-  Pp = r4(P)
+  Pp = r4(P) if esz == 4 else (P + 7) // 8 * 8
   Yp = r4(Y)
   NR, NE, MT = TY + 3, TY + 4, r4(TY + 2) + 8
   NRZ, NEZ, NRP = NR * Z, NE * Z, NR * Pp
@@ -645,6 +709,16 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
     return Ptr(base, stride, base, base + n,
                lambda c, y: tag(kind + c, level, plane, y))
 
+  if lean:  # one (buffer row, quad) item per thread over the NR rows
+    lthr, lra, lz0, lcol, lpml, _ = lean_items(Z, NR - 1, plo, phi)
+    lys = y0 - 2 + lra
+
+  def items(lo, hi, keep):
+    """Lean items whose buffer row is in [lo, hi) and whose domain row
+    `keep` admits: (thread, quad start, PML column, PML warp), rows, ys."""
+    sel = (lra >= lo) & (lra < hi) & keep(lys)
+    return (lthr[sel], lz0[sel], lcol[sel], lpml[sel]), lra[sel], lys[sel]
+
   for x in range(a1, xe + 1):
     l1, l2, st2 = x <= last1, x - 1 >= a2, x - 1 >= xs
     b = x & 1
@@ -665,6 +739,18 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
       Ho = Ptr(As + a_h, NRZ, *a_rng, lambda c, y, x=x: tag(H + c, 0, x, y))
       Pin = Ptr(As + a_p, NRP, *a_rng, lambda c, y, x=x: tag(PSI + c, 0, x, y))
       ras, ys, thr = phase_rows(0, NR, ydom, lambda y: 0 <= y < Y, rpt, Zh, z0s)
+      if lean:
+        it, ra_, y_ = items(0, NR, lambda y: (y >= 0) & (y < Y))
+        h_quad(sm, "L1 H", it, Z, Y, Pp, ra_, y_, Ep, E1p, Ho, Pin)
+        ie = ra_ * Z + it[1]
+        for c in range(3):
+          sm.write("L1 H out", h1c + c * NRZ + ie, it[0], tag(H + c, 1, x, y_), h1c,
+                   h1c + 3 * NRZ, 4)
+        m = it[3]
+        for c in range(2):
+          sm.write("L1 H psi", (p1c + c * NRP + ra_ * Pp + it[2])[m], it[0][m],
+                   tag(PSI + c, 1, x, y_[m]), p1c, p1c + 4 * NRP, 4)
+        ras = ras[:0]
       if len(ras):
         h_pair(sm, "L1 H", thr, z0s, pz, Z, Y, Pp, ras, ys, Ep, E1p, Ho, Pin)
         ra, y = ras[:, None], ys[:, None]
@@ -690,6 +776,22 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
       Pe = Ptr(As + a_p + 2 * NRP, NRP, As, As + a_stage,
                lambda c, y, x=x: tag(PSI + 2 + c, 0, x, y))
       ras, ys, thr = phase_rows(1, NR, ydom, lambda y: 0 <= y < Y, rpt, Zh, z0s)
+      if lean:
+        it, ra_, y_ = items(1, NR, lambda y: (y >= 0) & (y < Y))
+        for c in range(3):
+          sm.read("L1 E:mask", Ms + c * MT + ra_, it[0], tag(MASK + c, 0, x, y_),
+                  False, Bs + b_m + c * MT, Bs + b_m + c * MT + (mb - ma))
+        e_quad(sm, "L1 E", it, Z, Pp, ra_, y_, hc[0], hc[1], hc[2], hp[1], hp[2],
+               x == 0 or poison, Eo, Cb, Pe)
+        ie = ra_ * Z + it[1]
+        for c in range(3):
+          out = tag(POISON, 1, x, y_) if poison else tag(E + c, 1, x, y_)
+          sm.write("L1 E out", e1c + c * NRZ + ie, it[0], out, e1c, e1c + 3 * NRZ, 4)
+        m = it[3]
+        for c in (2, 3):
+          sm.write("L1 E psi", (p1c + c * NRP + ra_ * Pp + it[2])[m], it[0][m],
+                   tag(PSI + c, 1, x, y_[m]), p1c, p1c + 4 * NRP, 4)
+        ras = ras[:0]
       if len(ras):
         for c in range(3):
           sm.read("L1 E:mask", Ms + c * MT + ras, thr[:, 0], tag(MASK + c, 0, x, ys),
@@ -720,6 +822,17 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
       Ho = buf(h1p, NRZ, 3 * NRZ, H, 1, xm)
       Pin = buf(p1p, NRP, 4 * NRP, PSI, 1, xm)
       ras, ys, thr = phase_rows(1, NR - 1, ydom, lambda y: 0 <= y < Y, rpt, Zh, z0s)
+      if lean:
+        it, ra_, y_ = items(1, NR - 1, lambda y: (y >= 0) & (y < Y))
+        h_quad(sm, "L2 H", it, Z, Y, Pp, ra_, y_, Ep, E1p, Ho, Pin)
+        ie = ra_ * Z + it[1]
+        sm.write("L2 Hx", H2x + ie, it[0], tag(H, 2, xm, y_), H2x, H2x + NRZ, 4)
+        for c in (1, 2):
+          sm.write("L2 Hyz", h2yz + (c - 1) * NRZ + ie, it[0], tag(H + c, 2, xm, y_),
+                   h2yz, h2yz + 2 * NRZ, 4)
+        if st2:
+          cover[0, xm, y_[ra_ >= 2]] += 1
+        ras = ras[:0]
       if len(ras):
         h_pair(sm, "L2 H", thr, z0s, pz, Z, Y, Pp, ras, ys, Ep, E1p, Ho, Pin)
         ra, y = ras[:, None], ys[:, None]
@@ -744,6 +857,15 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover):
       Pe = Ptr(p1p + 2 * NRP, NRP, p1p, p1p + 4 * NRP,
                lambda c, y: tag(PSI + 2 + c, 1, xm, y))
       ras, ys, thr = phase_rows(2, NR - 1, ydom, lambda y: y < Y, rpt, Zh, z0s)
+      if lean:
+        it, ra_, y_ = items(2, NR - 1, lambda y: y < Y)
+        for c in range(3):
+          sm.read("L2 E:mask", Ms + c * MT + ra_, it[0], tag(MASK + c, 0, xm, y_),
+                  False, Bm + b_m + c * MT, Bm + b_m + c * MT + (mb - ma))
+        e_quad(sm, "L2 E", it, Z, Pp, ra_, y_, hx, hy, hz, hyp, hzp, xm == 0, Eo, Cb,
+               Pe)
+        cover[1, xm, y_] += 1
+        ras = ras[:0]
       if len(ras):
         for c in range(3):
           sm.read("L2 E:mask", Ms + c * MT + ras, thr[:, 0], tag(MASK + c, 0, xm, ys),
@@ -789,9 +911,10 @@ def one_step(X, Y, Z, plo, phi, TY, S, seg_x, ncomp, src, plant=None, hbuf=2,
   return run_grid(cta, X, Y, TY, seg_x, (X, Y))
 
 
-def two_step(X, Y, Z, plo, phi, TY, SA, seg_x, ncomp):
+def two_step(X, Y, Z, plo, phi, TY, SA, seg_x, ncomp, lean=False, esz=4):
   def cta(tile, seg, cover):
-    return two_step_cta(X, Y, Z, plo, phi, TY, SA, SA, seg_x, tile, seg, ncomp, cover)
+    return two_step_cta(X, Y, Z, plo, phi, TY, SA, SA, seg_x, tile, seg, ncomp, cover,
+                        lean, esz)
   return run_grid(cta, X, Y, TY, seg_x, (2, X, Y))
 
 
@@ -1041,3 +1164,28 @@ def test_lean_geometry_bulk_copy_alignment(esz, Z, TY, P):
   # Quads (4 values) of every region are 16-byte (FP32) / 8-byte (binary16)
   # aligned: region starts are 16-byte aligned and rows hold whole quads.
   assert Z % 4 == 0 and g["Pp"] % 4 == 0
+
+
+@pytest.mark.parametrize("esz", [4, 2])
+@pytest.mark.parametrize("X,Y,Z,TY", [(6, 40, 64, 14), (5, 23, 64, 14),
+                                      (7, 31, 32, 8), (4, 11, 16, 5)])
+@pytest.mark.parametrize("plo,phi", [(0, 0), (8, 8), (4, 12)])
+def test_lean_two_step_compute_accesses(X, Y, Z, TY, plo, phi, esz):
+  """The lean two-step kernel (one quad item per thread over the NR = TY+3
+  rows of level 1, interior and PML warps) under the two-step kernel's ring
+  protocol: every shared access in bounds and quad-aligned, every read the
+  exact data (field, level, plane, row) its update needs, no race between
+  barriers, every level-1 and level-2 row of the launch stored once."""
+  if plo + phi > Z:
+    pytest.skip("slabs wider than the domain")
+  checked = 0
+  for SA, seg_x in itertools.product((2, 3), (1, 3, X)):
+    res = two_step(X, Y, Z, plo, phi, TY, SA, seg_x, min_ncomp(Z), lean=True,
+                   esz=esz)
+    if res is None:
+      continue
+    reads, bad, cover = res
+    assert not bad, (X, Y, Z, TY, plo, phi, SA, seg_x, bad[:3])
+    assert (cover == 1).all(), (SA, seg_x)
+    checked += reads
+  assert checked > 0
