@@ -244,6 +244,33 @@ int32_t pjzfdtd_plan_launch_config(const pjzfdtd_plan* plan, int32_t* tile_y,
                                    int32_t* steps_per_pass, int32_t* kernel,
                                    int32_t* stages);
 
+/* Weighted port-plane sums of recorded phasors, for S-matrix entries:
+   out[k][w] = sum_p (blocks[k][w][comps[k]][p] + i blocks[k][ww+w][comps[k]][p])
+   * profiles[k][p], FP64 accumulation in a fixed order.  blocks[k] points at
+   one monitor box of a PHASORS output, (2 ww, 3, npts[k]) floats (device);
+   profiles[k]: device (npts[k]); out: device (nterms, ww, 2) doubles;
+   1 <= nterms <= 64, ww <= 32.  Replaces the transverse-slice overlap sums
+   of pjz's scatter (src/pjz/_field.py:305-338, 367-369) on the device.
+   Stream-ordered, no workspace. */
+int32_t pjzfdtd_plane_overlaps(int32_t nterms, const float* const* blocks,
+                               const float* const* profiles,
+                               const int32_t* comps, const int64_t* npts,
+                               int32_t ww, double* out, void* stream);
+
+/* dL/d-eps of a multi-port S-matrix objective from one batched launch:
+   grad[t] = sum_w Re(q[w] sum_i forward_i,w[t] sum_j coef[i][j][w]
+   adjoint_j,w[t]), FP64 sums, over `cells` = 3 x (design box) cells.
+   forward[i] / adjoint[j]: device phasors (2 ww, cells) of forward solve i
+   and unit-adjoint solve j (host arrays of n device pointers); coef: host
+   (n, n, ww, 2) floats = conj(dL/dS_ij); q: host (ww, 2) floats; grad:
+   device (cells).  n <= 16, ww <= 32, n*n*ww <= 1024.  Replaces the
+   reciprocity residual product of pjz's scatter VJP
+   (src/pjz/_field.py:380-398).  Stream-ordered, no workspace. */
+int32_t pjzfdtd_smatrix_gradient(int32_t n, int32_t ww, int64_t cells,
+                                 const float* const* forward,
+                                 const float* const* adjoint, const float* coef,
+                                 const float* q, float* grad, void* stream);
+
 /* Permittivity of the Yee cell from magnified layer profiles: pjz's
    `epsilon(layers, interface_positions, magnification, zz,
    use_simple_averaging)` (src/pjz/_epsilon.py:104-155) on the GPU, so a

@@ -67,6 +67,9 @@ SIGNATURES = {
     "pjzfdtd_batch_run": (_I, [_P, _P, _P, ctypes.c_size_t, _I, _P]),
     "pjzfdtd_batch_destroy": (_I, [_P]),
     "pjzfdtd_render_epsilon": (_I, [_P, _I, _I, _I, _I, _I, _P, _I, _P, _P]),
+    "pjzfdtd_plane_overlaps": (_I, [_I, _P, _P, _P, _P, _I, _P, _P]),
+    "pjzfdtd_smatrix_gradient": (_I, [_I, _I, ctypes.c_int64, _P, _P, _P, _P, _P,
+                                      _P]),
 }
 
 _lib = None

@@ -303,17 +303,17 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const bool zhi = z0 + 4 < Z;  // a z + 1 neighbour inside the domain
   const bool zlo = z0 > 0;      // a z - 1 neighbour inside the domain
 
-  float ike[4], ikh[4], be[4], ce[4], bh[4], ch[4];
+  float ike[4], ikh[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int z = min(z0 + k, Z - 1);  // idle lanes read a valid entry
     ike[k] = a.zc[z];
     ikh[k] = a.zc[3 * Z + z];
-    be[k] = pml ? a.zc[Z + z] : 0.f;
-    ce[k] = pml ? a.zc[2 * Z + z] : 0.f;
-    bh[k] = pml ? a.zc[4 * Z + z] : 0.f;
-    ch[k] = pml ? a.zc[5 * Z + z] : 0.f;
   }
+  // CPML decay / coupling of the quad's cells (PML warps only), read where
+  // used from the coefficient table (cached), which keeps them out of the
+  // register budget.
+  const float* zq = a.zc + min(z0, Z - 4);
   const float mdt = -a.dt;
   // Source box rows and z range of this item (the plane test is separate).
   const bool src_row = a.snc > 0 && yE >= a.sy0 && yE < a.sy0 + a.sny &&
@@ -389,8 +389,9 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dEy_x = fsub(e1y[j], ey[j]), dEx_y = fsub(exy[j], ex[j]);
         float zEy, zEx;
         if (pml) {
-          const float na = ffma(ch[j], dEy_z, fmul(bh[j], pa[j]));
-          const float nb = ffma(ch[j], dEx_z, fmul(bh[j], pb[j]));
+          const float bh = __ldg(zq + 4 * Z + j), ch = __ldg(zq + 5 * Z + j);
+          const float na = ffma(ch, dEy_z, fmul(bh, pa[j]));
+          const float nb = ffma(ch, dEx_z, fmul(bh, pb[j]));
           pa[j] = na;
           pb[j] = nb;
           zEy = ffma(dEy_z, ikh[j], na);
@@ -416,7 +417,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 
     // E^{n+1}(x) of the quad at tile row rH (y = y0 + rH).
     if (x >= xs && doE) {
-      float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4], eo[3][4], cb[3][4];
+      float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4];
       Q::ld(hcur + ihE, hx);
       Q::ld(hcur + RHZ + ihE, hy);
       Q::ld(hcur + 2 * RHZ + ihE, hz);
@@ -426,11 +427,6 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       const float hyz = zlo ? Q::ld1(hcur + RHZ + ihE - 1) : 0.f;
       Q::ld(hprev + RHZ + ihE, hyp);
       Q::ld(hprev + 2 * RHZ + ihE, hzp);
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Q::ld(Es + c * REZ + ihE, eo[c]);
-        Q::ld(Cs + c * TYZ + icE, cb[c]);
-      }
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
       float pa[4], pb[4];
       if (pml) {
@@ -438,7 +434,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         Q::ld(Ps + 3 * RH * Pp + pE, pb);
       }
       const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
-      float enew[3][4];
+      float cur[3][4];  // curl H - J of the quad's cells
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const float hy0 = j > 0 ? hy[j - 1] : hyz;
@@ -448,8 +444,9 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dHy_x = fsub(hy[j], hyp[j]), dHx_y = fsub(hx[j], hxm[j]);
         float zHy, zHx;
         if (pml) {
-          const float na = ffma(ce[j], dHy_z, fmul(be[j], pa[j]));
-          const float nb = ffma(ce[j], dHx_z, fmul(be[j], pb[j]));
+          const float be = __ldg(zq + Z + j), ce = __ldg(zq + 2 * Z + j);
+          const float na = ffma(ce, dHy_z, fmul(be, pa[j]));
+          const float nb = ffma(ce, dHx_z, fmul(be, pb[j]));
           pa[j] = na;
           pb[j] = nb;
           zHy = ffma(dHy_z, ike[j], na);
@@ -458,7 +455,9 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
           zHy = fmul(dHy_z, ike[j]);
           zHx = fmul(dHx_z, ike[j]);
         }
-        float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
+        cur[0][j] = fsub(dHz_y, zHy);
+        cur[1][j] = fsub(zHx, dHz_x);
+        cur[2][j] = fsub(dHy_x, dHx_y);
         if (src) {
           const int z = z0 + j;
           if (z >= a.sz0 && z < a.sz0 + a.snz) {
@@ -469,18 +468,24 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
               float jc = 0.f;
               for (int w = 0; w < a.snc; ++w)
                 jc = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], jc);
-              cur[c] = fsub(cur[c], jc);
+              cur[c][j] = fsub(cur[c][j], jc);
             }
           }
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float rr = ffma(-sig[c], eo[c][j], cur[c]);
-          enew[c][j] = ffma(cb[c][j], rr, eo[c][j]);
-        }
       }
+      // One component at a time: old E and its coefficient, the update.
 #pragma unroll
-      for (int c = 0; c < 3; ++c) Q::st(ecur + c * TYZ + icE, enew[c]);
+      for (int c = 0; c < 3; ++c) {
+        float eo[4], cb[4], en[4];
+        Q::ld(Es + c * REZ + ihE, eo);
+        Q::ld(Cs + c * TYZ + icE, cb);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float rr = ffma(-sig[c], eo[j], cur[c][j]);
+          en[j] = ffma(cb[j], rr, eo[j]);
+        }
+        Q::st(ecur + c * TYZ + icE, en);
+      }
       if (pml) {
         Q::st(pcur + 2 * TY * Pp + rH * Pp + col, pa);
         Q::st(pcur + 3 * TY * Pp + rH * Pp + col, pb);
@@ -505,8 +510,18 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 // for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
 #define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
 
+// Block bound of a lean kernel instantiation: binary16 tiles need half the
+// shared memory, so two CTAs share an SM (at most 320 threads each, so that
+// their registers fit); FP32 tiles run one CTA per SM.
+template <typename T>
+struct LeanBounds {
+  static constexpr int threads = sizeof(T) == 2 ? 320 : 384;
+  static constexpr int blocks = sizeof(T) == 2 ? 2 : 1;
+};
+
 template <int ZC, int TYC, typename T>
-__global__ void __launch_bounds__(384, 1) yee_lean_kernel(const StreamArgs sa) {
+__global__ void __launch_bounds__(LeanBounds<T>::threads, LeanBounds<T>::blocks)
+    yee_lean_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) unsigned char lean_sm[];
   lean_tile<ZC, TYC, T>(sa, blockIdx.x, blockIdx.y, lean_sm);
 }

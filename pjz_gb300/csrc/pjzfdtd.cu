@@ -26,6 +26,7 @@
 #include "lean_kernel.cuh"
 #include "lean2_kernel.cuh"
 #include "record_kernel.cuh"
+#include "smatrix_kernel.cuh"
 #include "kernel_table.cuh"
 
 using namespace pjzfdtd;
@@ -315,7 +316,9 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   }
   const int warps = lean_warps_interior(Z, ty, p.pml_lo, p.pml_hi) +
                     lean_warps_pml(ty, p.pml_lo, p.pml_hi);
-  if (warps * 32 + 32 > kLeanThreads)
+  const int bound = p.storage == PJZFDTD_STORAGE_F16 ? LeanBounds<__half>::threads
+                                                     : LeanBounds<float>::threads;
+  if (warps * 32 + 32 > bound)
     return required ? fail(PJZFDTD_ERR_UNSUPPORTED, "lean tile needs %d warps",
                            warps)
                     : PJZFDTD_OK;
@@ -1262,6 +1265,68 @@ int32_t pjzfdtd_batch_run(pjzfdtd_batch* batch, const pjzfdtd_buffers* buffers,
 
 int32_t pjzfdtd_batch_destroy(pjzfdtd_batch* batch) {
   delete batch;
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_plane_overlaps(int32_t nterms, const float* const* blocks,
+                               const float* const* profiles,
+                               const int32_t* comps, const int64_t* npts,
+                               int32_t ww, double* out, void* stream) {
+  if (nterms < 1 || nterms > kPlaneTermsMax)
+    return fail(PJZFDTD_ERR_INVALID, "plane overlaps: 1 to %d terms, got %d",
+                kPlaneTermsMax, nterms);
+  if (ww < 1 || ww > kSmatFreqMax || !blocks || !profiles || !comps || !npts || !out)
+    return fail(PJZFDTD_ERR_INVALID, "plane overlaps: bad arguments");
+  PlaneOverlapArgs a = {};
+  for (int k = 0; k < nterms; ++k) {
+    if (!blocks[k] || !profiles[k] || npts[k] < 1 || comps[k] < 0 || comps[k] > 2)
+      return fail(PJZFDTD_ERR_INVALID, "plane overlaps: bad term %d", k);
+    a.block[k] = blocks[k];
+    a.prof[k] = profiles[k];
+    a.npts[k] = npts[k];
+    a.comp[k] = comps[k];
+  }
+  a.ww = ww;
+  a.out = out;
+  plane_overlap_kernel<<<dim3((unsigned)nterms, (unsigned)ww), kOverlapThreads, 0,
+                         static_cast<cudaStream_t>(stream)>>>(a);
+  CUDA_TRY(cudaGetLastError());
+  return PJZFDTD_OK;
+}
+
+int32_t pjzfdtd_smatrix_gradient(int32_t n, int32_t ww, int64_t cells,
+                                 const float* const* forward,
+                                 const float* const* adjoint, const float* coef,
+                                 const float* q, float* grad, void* stream) {
+  if (n < 1 || n > kSmatSolvesMax || ww < 1 || ww > kSmatFreqMax ||
+      (long long)n * n * ww > kSmatCoefMax)
+    return fail(PJZFDTD_ERR_INVALID,
+                "S-matrix gradient: n <= %d, ww <= %d and n*n*ww <= %d, got "
+                "n=%d ww=%d", kSmatSolvesMax, kSmatFreqMax, kSmatCoefMax, n, ww);
+  if (cells < 1 || !forward || !adjoint || !coef || !q || !grad)
+    return fail(PJZFDTD_ERR_INVALID, "S-matrix gradient: bad arguments");
+  SmatGradArgs a = {};
+  for (int i = 0; i < n; ++i) {
+    if (!forward[i] || !adjoint[i])
+      return fail(PJZFDTD_ERR_INVALID, "S-matrix gradient: NULL phasors %d", i);
+    a.F[i] = forward[i];
+    a.G[i] = adjoint[i];
+  }
+  for (int k = 0; k < n * n * ww; ++k) {
+    a.coef[k][0] = coef[2 * k];
+    a.coef[k][1] = coef[2 * k + 1];
+  }
+  for (int w = 0; w < ww; ++w) {
+    a.q[w][0] = q[2 * w];
+    a.q[w][1] = q[2 * w + 1];
+  }
+  a.n = n;
+  a.ww = ww;
+  a.cells = cells;
+  a.grad = grad;
+  const int blocks = (int)std::min<long long>((cells + 255) / 256, 1 << 16);
+  smatrix_grad_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  CUDA_TRY(cudaGetLastError());
   return PJZFDTD_OK;
 }
 

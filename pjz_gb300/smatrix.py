@@ -23,12 +23,13 @@ the recorded boxes of every solve (the design box and the monitor planes, a
 few MB), and every rank assembles the same S, objective and gradient.
 """
 
+import ctypes
 from typing import List, NamedTuple, Tuple
 
 import numpy as np
 import torch
 
-from . import _adjoint, _field, engine, replicas
+from . import _adjoint, _field, _lib, engine, replicas
 from .workloads import (ABSORBER_COEFF, EPS_SI, EPS_SIO2, _blur,
                         _slab_fraction, omega_of)
 
@@ -239,30 +240,54 @@ class SMatrixSolver:
 
   def results(self):
     """(S (n, n, ww) complex, objective, dL/d-eps (3, design box)); with
-    several ranks every rank must call it (it starts with the exchange)."""
+    several ranks every rank must call it (it starts with the exchange).
+
+    Both reductions run on the device in the native library: S_ij is one
+    weighted sum over port j's monitor plane of forward i's phasors
+    (``pjzfdtd_plane_overlaps``), and dL/d-eps is
+    ``sum_w Re(q_w sum_ij F_i c_ij G_j)`` over the design box
+    (``pjzfdtd_smatrix_gradient``), both in FP64; only the n x n x ww
+    objective and its coefficients ``c = conj(dL/dS)`` are formed on the
+    host."""
     self.exchange()
     P = self.P
+    lib = _lib.load()
     n, ww = len(P.ports), len(P.omega)
-    cplx = lambda a: torch.complex(a[:ww], a[ww:])  # (2ww, 3, ...) -> (ww, ...)
-    F_design, S = [], torch.zeros((n, n, ww), dtype=torch.complex128,
-                                  device=self.dev)
+    dev = self.dev
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
+    # Overlaps: term (i, j) = forward i's phasors on port j's plane.
+    blocks, profs, comps, npts = [], [], [], []
+    prof_t = [torch.as_tensor(_port_profile(P, port), device=dev).reshape(-1)
+              .contiguous() for port in P.ports]
+    views = [self.plans[i].split(self.outs[i]) for i in range(n)]
     for i in range(n):
-      views = self.plans[i].split(self.outs[i])
-      F_design.append(cplx(views[0]))
       for j, port in enumerate(P.ports):
-        e = cplx(views[1 + j])[:, _transverse(port)].to(torch.complex128)
-        p = torch.as_tensor(_port_profile(P, port), device=self.dev,
-                            dtype=torch.float64).reshape(e.shape[1:])
-        S[i, j] = (e * p).sum(dim=(-3, -2, -1))
-    G = [cplx(self.plans[n + j].split(self.outs[n + j])[0]) for j in range(n)]
-    m = torch.as_tensor(P.target, device=self.dev, dtype=torch.float64)
-    L = (m[:, :, None] * S.abs() ** 2).sum()
-    c = torch.conj(2 * m[:, :, None] * S)  # (n, n, ww)
+        v = views[i][1 + j]
+        blocks.append(v.data_ptr())
+        profs.append(prof_t[j].data_ptr())
+        comps.append(_transverse(port))
+        npts.append(v[0, 0].numel())
+    S_dev = torch.empty((n * n, ww, 2), dtype=torch.float64, device=dev)
+    arr = lambda t, v: (t * len(v))(*v)
+    _lib.check(lib.pjzfdtd_plane_overlaps(
+        n * n, arr(ctypes.c_void_p, blocks), arr(ctypes.c_void_p, profs),
+        arr(ctypes.c_int32, comps), arr(ctypes.c_int64, npts), ww,
+        ctypes.c_void_p(S_dev.data_ptr()), stream))
+    S = torch.view_as_complex(S_dev).reshape(n, n, ww)
+    Sh = S.cpu().numpy()
+    m = np.asarray(P.target, np.float64)
+    L = torch.as_tensor((m[:, :, None] * np.abs(Sh) ** 2).sum(), dtype=torch.float64)
+    c = np.conj(2 * m[:, :, None] * Sh)  # (n, n, ww)
     wt = _adjoint.discrete_omega(P.omega, 0.5)
-    q = torch.as_tensor(wt**2 * np.exp(-2j * P.omega * 0.5), device=self.dev,
-                        dtype=torch.complex128)
-    F = torch.stack(F_design).to(torch.complex128)  # (n, ww, 3, box)
-    Gs = torch.stack(G).to(torch.complex128)
-    cg = torch.einsum("ijw,jwcxyz->iwcxyz", c, Gs)
-    grad = torch.einsum("w,iwcxyz->cxyz", q, F * cg).real
-    return S, L, grad.to(torch.float32)
+    q = wt**2 * np.exp(-2j * P.omega * 0.5)
+    F = [views[i][0] for i in range(n)]
+    G = [self.plans[n + j].split(self.outs[n + j])[0] for j in range(n)]
+    cells = int(F[0][0].numel())
+    grad = torch.empty(F[0].shape[1:], dtype=torch.float32, device=dev)
+    cf = np.ascontiguousarray(np.stack([c.real, c.imag], -1), np.float32)
+    qf = np.ascontiguousarray(np.stack([q.real, q.imag], -1), np.float32)
+    _lib.check(lib.pjzfdtd_smatrix_gradient(
+        n, ww, cells, arr(ctypes.c_void_p, [t.data_ptr() for t in F]),
+        arr(ctypes.c_void_p, [t.data_ptr() for t in G]), cf.ctypes.data,
+        qf.ctypes.data, ctypes.c_void_p(grad.data_ptr()), stream))
+    return S, L, grad

@@ -76,3 +76,41 @@ def test_smatrix_matches_fp64_oracle_and_finite_differences(native):
   err = np.linalg.norm(fd - ad) / np.linalg.norm(fd)
   print("FP64 S-matrix gradient vs FD:", err, fd, ad)
   assert err < 1e-3
+
+
+def test_device_assembly_matches_torch_restatement(native):
+  """S, objective and gradient from the device kernels (plane overlaps and
+  the FP64 gradient product) against the same sums written as complex128
+  torch reductions over the same recorded phasors."""
+  import numpy as _np
+  from pjz_gb300 import _adjoint
+  P = _tiny()
+  s = smatrix.SMatrixSolver(P)
+  s.run_batched()
+  S, L, grad = s.results()
+  n, ww = len(P.ports), len(P.omega)
+  cplx = lambda a: torch.complex(a[:ww], a[ww:])
+  Sref = torch.zeros((n, n, ww), dtype=torch.complex128, device=S.device)
+  F = []
+  for i in range(n):
+    views = s.plans[i].split(s.outs[i])
+    F.append(cplx(views[0]).to(torch.complex128))
+    for j, port in enumerate(P.ports):
+      e = cplx(views[1 + j])[:, smatrix._transverse(port)].to(torch.complex128)
+      p = torch.as_tensor(smatrix._port_profile(P, port), device=S.device,
+                          dtype=torch.float64).reshape(e.shape[1:])
+      Sref[i, j] = (e * p).sum(dim=(-3, -2, -1))
+  G = torch.stack([cplx(s.plans[n + j].split(s.outs[n + j])[0]) for j in range(n)]
+                  ).to(torch.complex128)
+  m = torch.as_tensor(P.target, device=S.device, dtype=torch.float64)
+  Lref = (m[:, :, None] * Sref.abs() ** 2).sum()
+  c = torch.conj(2 * m[:, :, None] * Sref)
+  wt = _adjoint.discrete_omega(P.omega, 0.5)
+  q = torch.as_tensor(wt**2 * _np.exp(-2j * P.omega * 0.5), device=S.device,
+                      dtype=torch.complex128)
+  cg = torch.einsum("ijw,jwcxyz->iwcxyz", c, G)
+  gref = torch.einsum("w,iwcxyz->cxyz", q, torch.stack(F) * cg).real
+  torch.testing.assert_close(S, Sref, rtol=1e-12, atol=0)
+  assert abs(float(L) - float(Lref)) <= 1e-12 * float(Lref)
+  # coefficients pass as float32 into the kernel; FP64 sums otherwise
+  torch.testing.assert_close(grad.double(), gref, rtol=1e-5, atol=1e-6 * float(gref.abs().max()))

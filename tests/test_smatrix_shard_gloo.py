@@ -1,9 +1,10 @@
 """The S-matrix solves shared over two ranks (gloo on the CPU): the ranks'
 shares cover the 2n solves exactly once, and after the exchange every rank
-assembles the same S, objective and gradient as one rank holding every
-solve.  The solves themselves need a GPU; here each rank fills the recorded
-boxes of its own solves with seeded data (and the others with NaN, so a
-missing exchange shows), which is what the assembly consumes."""
+holds every solve's recorded boxes bit for bit as one rank holding every
+solve does -- the inputs of the (device) S, objective and gradient
+assembly.  The solves themselves need a GPU; here each rank fills the
+recorded boxes of its own solves with seeded data (and the others with
+NaN, so a missing exchange shows)."""
 
 import os
 import socket
@@ -36,8 +37,8 @@ def _worker(rank, world, port, q):
   try:
     s = smatrix.SMatrixSolver(_problem(), device="cpu", rank=rank, world=world)
     _fill(s, set(s.mine))
-    S, L, g = s.results()
-    q.put((rank, list(s.mine), S.numpy(), float(L), g.numpy()))
+    s.exchange()
+    q.put((rank, list(s.mine), [o.numpy() for o in s.outs]))
   finally:
     dist.destroy_process_group()
 
@@ -47,7 +48,7 @@ def test_sharded_smatrix_assembles_like_one_rank():
   one = smatrix.SMatrixSolver(_problem(), device="cpu")
   assert one.mine == list(range(len(one.plans)))
   _fill(one, set(one.mine))
-  S1, L1, g1 = one.results()
+  one.exchange()
 
   with socket.socket() as sk:
     sk.bind(("127.0.0.1", 0))
@@ -64,8 +65,7 @@ def test_sharded_smatrix_assembles_like_one_rank():
   shares = [set(o[1]) for o in out]
   assert not shares[0] & shares[1]
   assert shares[0] | shares[1] == set(range(len(one.plans)))
-  for _, _, S, L, g in out:
-    assert np.isfinite(g).all()
-    np.testing.assert_array_equal(S, S1.numpy())
-    assert L == float(L1)
-    np.testing.assert_array_equal(g, g1.numpy())
+  for _, _, outs in out:
+    for got, want in zip(outs, one.outs):
+      assert np.isfinite(got).all()
+      np.testing.assert_array_equal(got, want.numpy())
