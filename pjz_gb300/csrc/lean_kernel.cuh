@@ -52,8 +52,9 @@ __host__ __device__ inline int lean_warps_pml(int ty, int plo, int phi) {
 // 0..TY-1 (all T), the absorber window (FP32) and the z-PML state rows (T,
 // row stride Pp = P rounded up to 16 bytes); every region starts on a
 // 16-byte boundary, as the bulk copies need.  After the ring: new H
-// [2][3][RH*Z], new E [2][3][TY*Z], new PML state [2][4][TY*Pp] (T), then
-// the mbarriers.  For T = float this is StreamGeom's layout.
+// [3][3][RH*Z] (planes x - 1, x, x + 1: the E phase of plane x shares its
+// barrier interval with the H phase of plane x + 1), new E [2][3][TY*Z],
+// new PML state [2][4][TY*Pp] (T), then the mbarriers.
 template <typename T>
 struct LeanGeom {
   int TY, Z, Pp, RE, RH, MT;
@@ -73,7 +74,7 @@ struct LeanGeom {
     p_off = m_off + 3 * MT * 4;
     stage = p_off + 4 * RH * Pp * (int)sizeof(T);
   }
-  __host__ __device__ size_t hn_bytes() const { return 2 * 3 * (size_t)RH * Z * sizeof(T); }
+  __host__ __device__ size_t hn_bytes() const { return 3 * 3 * (size_t)RH * Z * sizeof(T); }
   __host__ __device__ size_t en_bytes() const { return 2 * 3 * (size_t)TY * Z * sizeof(T); }
   __host__ __device__ size_t pn_bytes() const { return 2 * 4 * (size_t)TY * Pp * sizeof(T); }
   __host__ __device__ size_t bytes(int stages) const {
@@ -144,8 +145,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const int S = sa.stages;
   const LeanGeom<T> g(TY, Z, a.plo + a.phi);
   const int Pp = g.Pp;
-  T* hn = reinterpret_cast<T*>(sm + (size_t)S * g.stage);  // [2][3][RH*Z]
-  T* en = hn + 2 * 3 * RHZ;                                // [2][3][TY*Z]
+  T* hn = reinterpret_cast<T*>(sm + (size_t)S * g.stage);  // [3][3][RH*Z]
+  T* en = hn + 3 * 3 * RHZ;                                // [2][3][TY*Z]
   T* pn = en + 2 * 3 * TYZ;                                // [2][4][TY*Pp]
   uint64_t* full = reinterpret_cast<uint64_t*>(pn + 2 * 4 * TY * Pp);
   uint64_t* done = full + S;
@@ -248,7 +249,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
                               sa.wait_cycles);
       if (!ok) break;
       if (x >= xs) {
-        T* hcur = hn + (size_t)b * 3 * RHZ;
+        T* hcur = hn + (size_t)(k % 3) * 3 * RHZ;
         T* ecur = en + (size_t)b * 3 * TYZ;
         T* pcur = pn + (size_t)b * 4 * TY * Pp;
         const long long base = (long long)x * YZ + (long long)y0 * Z;
@@ -303,17 +304,17 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const bool zhi = z0 + 4 < Z;  // a z + 1 neighbour inside the domain
   const bool zlo = z0 > 0;      // a z - 1 neighbour inside the domain
 
-  float ike[4], ikh[4];
+  float ike[4], ikh[4], be[4], ce[4], bh[4], ch[4];
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
     const int z = min(z0 + k, Z - 1);  // idle lanes read a valid entry
     ike[k] = a.zc[z];
     ikh[k] = a.zc[3 * Z + z];
+    be[k] = pml ? a.zc[Z + z] : 0.f;
+    ce[k] = pml ? a.zc[2 * Z + z] : 0.f;
+    bh[k] = pml ? a.zc[4 * Z + z] : 0.f;
+    ch[k] = pml ? a.zc[5 * Z + z] : 0.f;
   }
-  // CPML decay / coupling of the quad's cells (PML warps only), read where
-  // used from the coefficient table (cached), which keeps them out of the
-  // register budget.
-  const float* zq = a.zc + min(z0, Z - 4);
   const float mdt = -a.dt;
   // Source box rows and z range of this item (the plane test is separate).
   const bool src_row = a.snc > 0 && yE >= a.sy0 && yE < a.sy0 + a.sny &&
@@ -326,37 +327,16 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const int pH = rH * Pp + col;
   const int pE = (rH + 1) * Pp + col;
 
-  int slot = 0, slot1 = S > 1 ? 1 : 0;  // ring slots of planes x and x+1
-  uint32_t round = 0, round1 = S > 1 ? 0 : 1;
-  for (int x = x0; x < xe; ++x) {
-    const int k = x - x0;
-    const int b = k & 1;
-    const bool has_x1 = x + 1 < X;
-    bool ok = true;
-    if (k == 0)
-      ok = mbar_wait_or_abort(&full[slot], round & 1, sa.status, &abort_flag,
-                              sa.wait_cycles);
-    if (ok && has_x1)
-      ok = mbar_wait_or_abort(&full[slot1], round1 & 1, sa.status, &abort_flag,
-                              sa.wait_cycles);
-    if (ok && k >= 2)
-      ok = mbar_wait_or_abort(&freeb[b], (uint32_t)((k >> 1) - 1) & 1, sa.status,
-                              &abort_flag, sa.wait_cycles);
-
-    const unsigned char* st = sm + (size_t)slot * g.stage;
+  // H^{n+1/2} of the quad at buffer row rH (y = y0 - 1 + rH) of the plane in
+  // ring slot `sl` (E of the next plane in slot `sl1`, or zero), into hcur /
+  // pcur (PML state comps 0, 1).
+  auto h_phase = [&](int sl, int sl1, bool has_x1, T* hcur, T* pcur) {
+    const unsigned char* st = sm + (size_t)sl * g.stage;
     const T* Es = reinterpret_cast<const T*>(st + g.e_off);
-    const T* E1 = reinterpret_cast<const T*>(sm + (size_t)slot1 * g.stage + g.e_off);
+    const T* E1 = reinterpret_cast<const T*>(sm + (size_t)sl1 * g.stage + g.e_off);
     const T* Hs = reinterpret_cast<const T*>(st + g.h_off);
-    const T* Cs = reinterpret_cast<const T*>(st + g.c_off);
-    const float* Ms = reinterpret_cast<const float*>(st + g.m_off) + moff;
     const T* Ps = reinterpret_cast<const T*>(st + g.p_off);
-    T* hcur = hn + (size_t)b * 3 * RHZ;
-    const T* hprev = hn + (size_t)(b ^ 1) * 3 * RHZ;
-    T* ecur = en + (size_t)b * 3 * TYZ;
-    T* pcur = pn + (size_t)b * 4 * TY * Pp;
-
-    // H^{n+1/2}(x) of the quad at buffer row rH (y = y0 - 1 + rH).
-    if (ok && doH) {
+    {
       float ex[4], ey[4], ez[4], exy[4], ezy[4], e1y[4], e1z[4], ho[3][4];
       Q::ld(Es + ieH, ex);
       Q::ld(Es + REZ + ieH, ey);
@@ -389,9 +369,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dEy_x = fsub(e1y[j], ey[j]), dEx_y = fsub(exy[j], ex[j]);
         float zEy, zEx;
         if (pml) {
-          const float bh = __ldg(zq + 4 * Z + j), ch = __ldg(zq + 5 * Z + j);
-          const float na = ffma(ch, dEy_z, fmul(bh, pa[j]));
-          const float nb = ffma(ch, dEx_z, fmul(bh, pb[j]));
+          const float na = ffma(ch[j], dEy_z, fmul(bh[j], pa[j]));
+          const float nb = ffma(ch[j], dEx_z, fmul(bh[j], pb[j]));
           pa[j] = na;
           pb[j] = nb;
           zEy = ffma(dEy_z, ikh[j], na);
@@ -412,12 +391,20 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         Q::st(pcur + TY * Pp + (rH - 1) * Pp + col, pb);
       }
     }
-    compute_sync(ncomp);
-    if (abort_flag) break;
+  };
 
-    // E^{n+1}(x) of the quad at tile row rH (y = y0 + rH).
-    if (x >= xs && doE) {
-      float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4];
+  // E^{n+1} of the quad at tile row rH (y = y0 + rH) of plane x in ring slot
+  // `sl`, from the new H of planes x (hcur) and x - 1 (hprev), into ecur /
+  // pcur (PML state comps 2, 3).
+  auto e_phase = [&](int x, int sl, const T* hcur, const T* hprev, T* ecur,
+                     T* pcur) {
+    const unsigned char* st = sm + (size_t)sl * g.stage;
+    const T* Es = reinterpret_cast<const T*>(st + g.e_off);
+    const T* Cs = reinterpret_cast<const T*>(st + g.c_off);
+    const float* Ms = reinterpret_cast<const float*>(st + g.m_off) + moff;
+    const T* Ps = reinterpret_cast<const T*>(st + g.p_off);
+    {
+      float hx[4], hy[4], hz[4], hxm[4], hzm[4], hyp[4], hzp[4], eo[3][4], cb[3][4];
       Q::ld(hcur + ihE, hx);
       Q::ld(hcur + RHZ + ihE, hy);
       Q::ld(hcur + 2 * RHZ + ihE, hz);
@@ -427,6 +414,11 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       const float hyz = zlo ? Q::ld1(hcur + RHZ + ihE - 1) : 0.f;
       Q::ld(hprev + RHZ + ihE, hyp);
       Q::ld(hprev + 2 * RHZ + ihE, hzp);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        Q::ld(Es + c * REZ + ihE, eo[c]);
+        Q::ld(Cs + c * TYZ + icE, cb[c]);
+      }
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
       float pa[4], pb[4];
       if (pml) {
@@ -434,7 +426,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         Q::ld(Ps + 3 * RH * Pp + pE, pb);
       }
       const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
-      float cur[3][4];  // curl H - J of the quad's cells
+      float enew[3][4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const float hy0 = j > 0 ? hy[j - 1] : hyz;
@@ -444,9 +436,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dHy_x = fsub(hy[j], hyp[j]), dHx_y = fsub(hx[j], hxm[j]);
         float zHy, zHx;
         if (pml) {
-          const float be = __ldg(zq + Z + j), ce = __ldg(zq + 2 * Z + j);
-          const float na = ffma(ce, dHy_z, fmul(be, pa[j]));
-          const float nb = ffma(ce, dHx_z, fmul(be, pb[j]));
+          const float na = ffma(ce[j], dHy_z, fmul(be[j], pa[j]));
+          const float nb = ffma(ce[j], dHx_z, fmul(be[j], pb[j]));
           pa[j] = na;
           pb[j] = nb;
           zHy = ffma(dHy_z, ike[j], na);
@@ -455,9 +446,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
           zHy = fmul(dHy_z, ike[j]);
           zHx = fmul(dHx_z, ike[j]);
         }
-        cur[0][j] = fsub(dHz_y, zHy);
-        cur[1][j] = fsub(zHx, dHz_x);
-        cur[2][j] = fsub(dHy_x, dHx_y);
+        float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
         if (src) {
           const int z = z0 + j;
           if (z >= a.sz0 && z < a.sz0 + a.snz) {
@@ -468,41 +457,85 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
               float jc = 0.f;
               for (int w = 0; w < a.snc; ++w)
                 jc = ffma(a.src[((long long)w * 3 + c) * sb + si], a.wave[w], jc);
-              cur[c][j] = fsub(cur[c][j], jc);
+              cur[c] = fsub(cur[c], jc);
             }
           }
         }
-      }
-      // One component at a time: old E and its coefficient, the update.
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float eo[4], cb[4], en[4];
-        Q::ld(Es + c * REZ + ihE, eo);
-        Q::ld(Cs + c * TYZ + icE, cb);
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const float rr = ffma(-sig[c], eo[j], cur[c][j]);
-          en[j] = ffma(cb[j], rr, eo[j]);
+        for (int c = 0; c < 3; ++c) {
+          const float rr = ffma(-sig[c], eo[c][j], cur[c]);
+          enew[c][j] = ffma(cb[c][j], rr, eo[c][j]);
         }
-        Q::st(ecur + c * TYZ + icE, en);
       }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) Q::st(ecur + c * TYZ + icE, enew[c]);
       if (pml) {
         Q::st(pcur + 2 * TY * Pp + rH * Pp + col, pa);
         Q::st(pcur + 3 * TY * Pp + rH * Pp + col, pb);
       }
     }
+  };
+
+  // Ring position (slot, fill round) of a plane, advanced plane by plane.
+  struct RingPos {
+    int slot;
+    uint32_t round;
+  };
+  auto next = [&](RingPos p) {
+    if (++p.slot == S) {
+      p.slot = 0;
+      ++p.round;
+    }
+    return p;
+  };
+  // Planes x, x + 1, x + 2 of the loop below.
+  RingPos p0 = {0, 0u};
+  RingPos p1 = next(p0);
+  RingPos p2 = next(p1);
+  T* const hbuf[3] = {hn, hn + 3 * RHZ, hn + 6 * RHZ};
+
+  // Plane x0: its H phase.
+  {
+    bool ok = mbar_wait_or_abort(&full[p0.slot], p0.round & 1, sa.status,
+                                 &abort_flag, sa.wait_cycles);
+    if (ok && x0 + 1 < X)
+      ok = mbar_wait_or_abort(&full[p1.slot], p1.round & 1, sa.status, &abort_flag,
+                              sa.wait_cycles);
+    if (ok && doH) h_phase(p0.slot, p1.slot, x0 + 1 < X, hbuf[0], pn);
+  }
+  // Each iteration: barrier (H of plane x done by every warp), E of plane x,
+  // release plane x to the producer, then H of plane x + 1 -- which needs
+  // no result of E(x), so the two share one barrier interval; three H
+  // buffers keep H(x + 1) off the H(x) and H(x - 1) that E(x) reads.
+  for (int x = x0; x < xe; ++x) {
+    const int k = x - x0;
+    compute_sync(ncomp);
+    if (abort_flag) break;
+    if (x >= xs && doE)
+      e_phase(x, p0.slot, hbuf[k % 3], hbuf[(k + 2) % 3],
+              en + (size_t)(k & 1) * 3 * TYZ, pn + (size_t)(k & 1) * 4 * TY * Pp);
     // Publish this plane's results to the producer and release its slot.
     fence_async_smem();
     __syncwarp();
-    if ((tid & 31) == 0) mbar_arrive(&done[slot]);
-    // H(x-1) (hprev) is rewritten by the next plane's H phase.
-    compute_sync(ncomp);
-    slot = slot1;
-    round = round1;
-    if (++slot1 == S) {
-      slot1 = 0;
-      ++round1;
+    if ((tid & 31) == 0) mbar_arrive(&done[p0.slot]);
+    if (x + 1 < xe) {
+      const int k1 = k + 1;
+      bool ok = true;
+      if (x + 2 < X)
+        ok = mbar_wait_or_abort(&full[p2.slot], p2.round & 1, sa.status,
+                                &abort_flag, sa.wait_cycles);
+      // The staging buffers of plane x + 1 held plane x - 1's results: wait
+      // until the producer's stores of them have read them.
+      if (ok && k1 >= 2)
+        ok = mbar_wait_or_abort(&freeb[k1 & 1], (uint32_t)((k1 >> 1) - 1) & 1,
+                                sa.status, &abort_flag, sa.wait_cycles);
+      if (ok && doH)
+        h_phase(p1.slot, p2.slot, x + 2 < X, hbuf[k1 % 3],
+                pn + (size_t)(k1 & 1) * 4 * TY * Pp);
     }
+    p0 = p1;
+    p1 = p2;
+    p2 = next(p2);
   }
 }
 
@@ -510,13 +543,13 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 // for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
 #define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
 
-// Block bound of a lean kernel instantiation: binary16 tiles need half the
-// shared memory, so two CTAs share an SM (at most 320 threads each, so that
-// their registers fit); FP32 tiles run one CTA per SM.
+// Block bound of a lean kernel instantiation (one CTA per SM: the ring and
+// staging buffers take most of the shared memory; two binary16 CTAs per SM
+// measured slower, their registers capped at 96 with spills).
 template <typename T>
 struct LeanBounds {
-  static constexpr int threads = sizeof(T) == 2 ? 320 : 384;
-  static constexpr int blocks = sizeof(T) == 2 ? 2 : 1;
+  static constexpr int threads = 384;
+  static constexpr int blocks = 1;
 };
 
 template <int ZC, int TYC, typename T>

@@ -322,12 +322,25 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
     return required ? fail(PJZFDTD_ERR_UNSUPPORTED, "lean tile needs %d warps",
                            warps)
                     : PJZFDTD_OK;
+  // The lean layout holds a third new-H buffer: drop ring stages (not
+  // below two, and only those picked automatically) where the streamed
+  // plan's depth no longer fits.
+  auto bytes = [&](int s) {
+    return p.storage == PJZFDTD_STORAGE_F16 ? LeanGeom<__half>(ty, Z, pl->P).bytes(s)
+                                            : LeanGeom<float>(ty, Z, pl->P).bytes(s);
+  };
+  int stages = pl->stages;
+  while (p.stages == 0 && stages > 2 && bytes(stages) > kSmemMax) --stages;
+  if (bytes(stages) > kSmemMax)
+    return required ? fail(PJZFDTD_ERR_UNSUPPORTED,
+                           "lean tile needs %zu bytes of shared memory",
+                           bytes(stages))
+                    : PJZFDTD_OK;
   pl->kernel = 3;
   pl->threads = warps * 32 + 32;
   pl->src_ring = pl->src_rows = 0;
-  pl->smem = p.storage == PJZFDTD_STORAGE_F16
-                 ? LeanGeom<__half>(ty, Z, pl->P).bytes(pl->stages)
-                 : LeanGeom<float>(ty, Z, pl->P).bytes(pl->stages);
+  pl->stages = stages;
+  pl->smem = bytes(stages);
   return PJZFDTD_OK;
 }
 

@@ -32,8 +32,9 @@ It mirrors the kernels' index arithmetic line for line (the shared helpers
 kernel change to that arithmetic must change this model with it.
 
 The lean one-step kernel (`csrc/lean_kernel.cuh`) shares the streamed
-kernel's layout and producer, so its replay is the one-step replay with the
-compute accesses swapped for the lean ones (`lean_items`, `lean_h`,
+kernel's producer and (with a third new-H buffer) its layout, so its replay
+is the one-step replay with three new-H buffers, one barrier per plane and
+the compute accesses swapped for the lean ones (`lean_items`, `lean_h`,
 `lean_e`): one z-quad per thread, 128-bit accesses (checked 16-byte
 aligned), interior and z-PML quads on separate warps.
 """
@@ -360,9 +361,9 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   `plant` puts a known mistake into the replay (for the tests that show the
   model catches it): "slot" reads plane x+1 from one ring slot too far,
   "moff" drops the absorber window offset.  `hbuf` (new-H buffers) and
-  `barriers` (named barriers per plane) are 2 and 2 in the kernel; other
-  values replay a candidate protocol: with one barrier the E phase of plane
-  x shares its interval with the H phase of plane x + 1.  The producer's
+  `barriers` (named barriers per plane) are 2 and 2 in the streamed kernel
+  and 3 and 1 in the lean kernel, where the E phase of plane x shares its
+  barrier interval with the H phase of plane x + 1.  The producer's
   stores of plane x are checked both right after its E phase and at the
   latest moment they may read, just before plane x + 2's wait on them."""
   P = plo + phi
@@ -1071,6 +1072,9 @@ def test_random_shapes():
                                                    nc2, res[1][:2])
 
 
+# The lean kernel's new-H buffers and barriers per plane.
+LEAN_PROTOCOL = dict(hbuf=3, barriers=1)
+
 LEAN_CASES = [(5, 30, 64, 14), (4, 41, 48, 19), (3, 61, 32, 29), (6, 9, 16, 5),
               (4, 13, 24, 3)]
 
@@ -1089,7 +1093,7 @@ def test_lean_compute_accesses(X, Y, Z, TY, plo, phi, esz):
   checked = 0
   for S, seg_x in itertools.product((2, 3, 4), (2, X)):
     res = one_step(X, Y, Z, plo, phi, TY, S, seg_x, min_ncomp(Z), None, lean=True,
-                   esz=esz)
+                   esz=esz, **LEAN_PROTOCOL)
     if res is None:
       continue
     reads, bad, cover = res
@@ -1119,17 +1123,21 @@ def test_lean_items_cover_each_quad_once():
 
 
 def test_lean_model_flags_a_planted_mistake():
-  """A lean replay whose absorber offset is dropped reads stale data."""
+  """A lean replay whose absorber offset is dropped reads stale data; one
+  barrier per plane with only two new-H buffers races."""
   args = (5, 30, 64, 8, 8, 14, 3, 2, 32, None)
-  assert one_step(*args, lean=True)[1] == []
-  res = one_step(*args, plant="moff", lean=True)
+  assert one_step(*args, lean=True, **LEAN_PROTOCOL)[1] == []
+  two = one_step(*args, lean=True, hbuf=2, barriers=1)
+  assert any(b[3] == "race" for b in two[1])  # H(x + 1) over H(x - 1)
+  res = one_step(*args, plant="moff", lean=True, **LEAN_PROTOCOL)
   assert any(b[2] == "LE:mask" and b[3] == "stale" for b in res[1])
 
 
 def lean_geom(TY, Z, P, esz):
   """Byte layout of a lean CTA (``LeanGeom`` in csrc/lean_kernel.cuh): slot
   regions E, H, coefficients (stored type), absorber (FP32), PML state
-  (stored type, rows of Pp values); then new H, new E, new PML state."""
+  (stored type, rows of Pp values); then new H (three buffers), new E, new
+  PML state."""
   per16 = 16 // esz
   Pp = (P + per16 - 1) // per16 * per16
   RE, RH, MT = TY + 2, TY + 1, r4(TY) + 8
@@ -1140,7 +1148,7 @@ def lean_geom(TY, Z, P, esz):
   p = m + 3 * MT * 4
   stage = p + 4 * RH * Pp * esz
   return dict(Pp=Pp, e=e, h=h, c=c, m=m, p=p, stage=stage,
-              hn=2 * 3 * RH * Z * esz, en=2 * 3 * TY * Z * esz,
+              hn=3 * 3 * RH * Z * esz, en=2 * 3 * TY * Z * esz,
               pn=2 * 4 * TY * Pp * esz)
 
 
