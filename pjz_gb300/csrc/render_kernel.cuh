@@ -34,9 +34,10 @@
 // pixel makes everything NaN), 0 * inf in the full mix gives NaN as pjz's
 // einsum does, so such columns take the full mix at every z.  FP32
 // throughout, the window sums in the order of the original per-window loop
-// (rows outer, columns inner); the per-cell functions are __host__
-// __device__ so that a host emulation of the block loop checks the same code
-// on the CPU.
+// (rows outer, columns inner).  The CTA's phases are __host__ __device__
+// strided loops over (thread, thread count), with no integer division in
+// their index arithmetic, so that a host emulation runs the kernel's own
+// code, thread by thread, on the CPU.
 #pragma once
 
 #include <math.h>
@@ -92,11 +93,51 @@ PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
 // window statistics [3][kRenderTileY][ll] of 4 floats, one-layer values
 // [3][kRenderTileY][ll], per (component, y) whether every layer's statistics
 // are finite [3][kRenderTileY] (int), the pixel patch and its reciprocals
-// [2][3m][2m*kRenderTileY + m], and the pixel offsets u [2m].
+// [2][3m][2m*kRenderTileY + m], the pixel offsets u [2m], the interface
+// positions [kRenderMaxLayers], and per component the z cells an interface
+// cuts [3][zz] (int) and their count [4] (int).
 PJZ_HD size_t render_smem_floats(int ll, int zz, int m) {
   return 6 * (size_t)ll * zz + 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
          3 * kRenderTileY +
-         2 * (size_t)render_patch_rows(m) * render_patch_cols(m) + 2 * m;
+         2 * (size_t)render_patch_rows(m) * render_patch_cols(m) + 2 * m +
+         kRenderMaxLayers + 3 * (size_t)zz + 4;
+}
+
+// The regions of one CTA's shared memory (render_smem_floats floats).
+struct RenderSmem {
+  float* frac;      // [3][ll][zz]
+  float* mid;       // [3][ll][zz]
+  int* owner;       // [3][zz]
+  WindowStats* st;  // [3][kRenderTileY][ll]
+  float* ival;      // [3][kRenderTileY][ll]
+  int* yfin;        // [3][kRenderTileY]
+  float* pf;        // [3m][pc]
+  float* pinv;      // [3m][pc]
+  float* u;         // [2m]
+  float* pos;       // [kRenderMaxLayers]
+  int* cut;         // [3][zz]: z cells no single layer fills
+  int* ncut;        // [4]: their number per component
+  float* end;
+};
+
+PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m) {
+  const int LZ = ll * zz, TL = kRenderTileY * ll;
+  const int np = render_patch_rows(m) * render_patch_cols(m);
+  RenderSmem s;
+  s.frac = sm;
+  s.mid = s.frac + 3 * LZ;
+  s.owner = reinterpret_cast<int*>(s.mid + 3 * LZ);
+  s.st = reinterpret_cast<WindowStats*>(s.owner + 3 * zz);
+  s.ival = reinterpret_cast<float*>(s.st + 3 * TL);
+  s.yfin = reinterpret_cast<int*>(s.ival + 3 * TL);
+  s.pf = reinterpret_cast<float*>(s.yfin + 3 * kRenderTileY);
+  s.pinv = s.pf + np;
+  s.u = s.pinv + np;
+  s.pos = s.u + 2 * m;
+  s.cut = reinterpret_cast<int*>(s.pos + kRenderMaxLayers);
+  s.ncut = s.cut + 3 * zz;
+  s.end = reinterpret_cast<float*>(s.ncut + 4);
+  return s;
 }
 
 PJZ_HD bool render_finite(const WindowStats& w) {
@@ -105,12 +146,13 @@ PJZ_HD bool render_finite(const WindowStats& w) {
 
 // Filled fraction of z cell `z` of component `c` by layer `l`, and the
 // offset of the filled part's midpoint from the cell centre.
-PJZ_HD void render_occupancy(const RenderArgs& a, int c, int l, int z,
-                             float* frac, float* mid) {
+// `pos` holds the interface positions.
+PJZ_HD void render_occupancy(const RenderArgs& a, const float* pos, int c, int l,
+                             int z, float* frac, float* mid) {
   const float lo = c == 2 ? (float)z : (float)z - 0.5f;
   const float hi = c == 2 ? (float)z + 1.0f : (float)z + 0.5f;
-  const float b = l == 0 ? lo : fminf(fmaxf(a.pos[l - 1], lo), hi);
-  const float t = l == a.ll - 1 ? hi : fminf(fmaxf(a.pos[l], lo), hi);
+  const float b = l == 0 ? lo : fminf(fmaxf(pos[l - 1], lo), hi);
+  const float t = l == a.ll - 1 ? hi : fminf(fmaxf(pos[l], lo), hi);
   *frac = (t - b) / (hi - lo);
   *mid = 0.5f * (b + t) - 0.5f * (lo + hi);
 }
@@ -152,21 +194,18 @@ PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
   return w;
 }
 
-// Stages pixel `t` of the patch of layer `l` for the CTA at (x, y0) with
-// ny tile rows: the pixel and its reciprocal.  Columns past the block's
-// windows (a short last tile) are left alone.
-PJZ_HD void render_stage(const RenderArgs& a, int l, int x, int y0, int ny, int t,
+// Stages row r, column cc of the patch of layer `l` for the CTA at (x, y0):
+// the pixel and its reciprocal.
+PJZ_HD void render_stage(const RenderArgs& a, int l, int x, int y0, int r, int cc,
                          float* pf, float* pinv) {
   const int k = 2 * a.m, pc = render_patch_cols(a.m);
-  const int r = t / pc, cc = t - r * pc;
-  if (cc >= k * ny + a.m) return;
   const int PX = k * a.xx, PY = k * a.yy;
   const int px = render_imax(k * x - a.m + r, 0);
   const int py = render_imax(k * y0 - a.m + cc, 0);
   const float* L = a.layers + (size_t)l * PX * PY;
   const float f = render_load(L, (size_t)px * PY + py);
-  pf[t] = f;
-  pinv[t] = 1.0f / f;
+  pf[r * pc + cc] = f;
+  pinv[r * pc + cc] = 1.0f / f;
 }
 
 // The value from the fraction-weighted sums over the layers.
@@ -214,58 +253,131 @@ PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) 
   return (((size_t)c * a.xx + x) * a.yy + y) * a.zz + z;
 }
 
+// The CTA's phases, each a strided loop of thread `tid` of `nthr` (a
+// barrier between consecutive phases), shared by the kernel and its host
+// emulation.  Phase 1: interface positions, pixel offsets, finiteness
+// flags.
+PJZ_HD void render_phase_setup(const RenderArgs& a, const RenderSmem& s, int tid,
+                               int nthr) {
+  if (tid == 0) {  // constant indices: the arguments stay in parameter space
+#pragma unroll
+    for (int i = 0; i < kRenderMaxLayers - 1; ++i)
+      s.pos[i] = i < a.ll - 1 ? a.pos[i] : 0.f;
+    s.pos[kRenderMaxLayers - 1] = 0.f;
+  }
+  for (int t = tid; t < 2 * a.m; t += nthr) s.u[t] = render_u(a, t);
+  for (int t = tid; t < 3 * kRenderTileY; t += nthr) s.yfin[t] = 1;
+}
+
+// Phase 2 (after the positions are in shared memory): z occupancy and the
+// filling layer of every component's z cells.
+PJZ_HD void render_phase_occupancy(const RenderArgs& a, const RenderSmem& s,
+                                   int tid, int nthr) {
+  const int LZ = a.ll * a.zz;
+  for (int c = 0; c < 3; ++c)
+    for (int z = tid; z < a.zz; z += nthr) {
+      for (int l = 0; l < a.ll; ++l)
+        render_occupancy(a, s.pos, c, l, z, &s.frac[c * LZ + l * a.zz + z],
+                         &s.mid[c * LZ + l * a.zz + z]);
+      s.owner[c * a.zz + z] = render_owner(a, s.frac + c * LZ, z);
+    }
+}
+
+// Phase 3 (beside the first layer's phase 4, after a barrier that follows
+// phase 2): per component, the z cells no single layer fills, in increasing
+// z, one thread per component.
+PJZ_HD void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
+                              int nthr) {
+  for (int c = tid; c < 3; c += nthr) {
+    int n = 0;
+    for (int z = 0; z < a.zz; ++z)
+      if (s.owner[c * a.zz + z] < 0) s.cut[c * a.zz + n++] = z;
+    s.ncut[c] = n;
+  }
+}
+
+// Phase 4, per layer: the pixel patch of the CTA at (x, y0) with ny tile
+// rows (the columns its windows cover: 2m*ny + m).
+PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l,
+                               int x, int y0, int ny, int tid, int nthr) {
+  const int cols = 2 * a.m * ny + a.m;
+  for (int r = 0; r < render_patch_rows(a.m); ++r)
+    for (int cc = tid; cc < cols; cc += nthr)
+      render_stage(a, l, x, y0, r, cc, s.pf, s.pinv);
+}
+
+// Phase 5, per layer: window statistics and one-layer values of the
+// (component, row) windows of the staged patch.
+PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l,
+                                 int ny, int tid, int nthr) {
+  const int pc = render_patch_cols(a.m);
+  for (int t = tid; t < 3 * ny; t += nthr) {
+    const int c = t >= 2 * ny ? 2 : (t >= ny ? 1 : 0), yl = t - c * ny;
+    const int cy = c * kRenderTileY + yl;
+    const int i = cy * a.ll + l;
+    s.st[i] = render_window(a, c, yl, s.pf, s.pinv, pc, s.u);
+    s.ival[i] = render_interior(a, c, s.st[i]);
+    if (!render_finite(s.st[i])) s.yfin[cy] = 0;  // any writer stores 0
+  }
+}
+
+// Phase 6: outputs.  Warp `w` of `nw` per (component, y) row, lane `lane`
+// of 32 along z (coalesced stores), writes the cells one layer fills; then
+// the CTA's threads share the interface-cut cells of every row (the same
+// few z for every row).  A row whose statistics are not all finite takes
+// the full mix at every z in the first loop.
+PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
+                             int y0, int ny, int w, int nw, int lane,
+                             float* out) {
+  const int LZ = a.ll * a.zz;
+  for (int c = 0; c < 3; ++c)
+    for (int yl = w; yl < ny; yl += nw) {
+      const int cy = c * kRenderTileY + yl;
+      const WindowStats* st = s.st + cy * a.ll;
+      float* row = out + render_out_index(a, c, x, y0 + yl, 0);
+      if (s.yfin[cy]) {
+        const float* iv = s.ival + cy * a.ll;
+        for (int z = lane; z < a.zz; z += 32) {
+          const int o = s.owner[c * a.zz + z];
+          if (o >= 0) row[z] = iv[o];
+        }
+      } else {
+        for (int z = lane; z < a.zz; z += 32)
+          row[z] = render_value(a, c, st, s.frac + c * LZ, s.mid + c * LZ, z);
+      }
+    }
+  const int tid = w * 32 + lane, nthr = nw * 32;
+  for (int c = 0; c < 3; ++c)
+    for (int t = tid; t < s.ncut[c] * kRenderTileY; t += nthr) {
+      const int yl = t % kRenderTileY, z = s.cut[c * a.zz + t / kRenderTileY];
+      const int cy = c * kRenderTileY + yl;
+      if (yl < ny && s.yfin[cy])
+        out[render_out_index(a, c, x, y0 + yl, z)] = render_value(
+            a, c, s.st + cy * a.ll, s.frac + c * LZ, s.mid + c * LZ, z);
+    }
+}
+
 #if defined(__CUDACC__) && defined(PJZ_RENDER_KERNEL)  // kern_render.cu only
-// grid (xx, ceil(yy / kRenderTileY)); dynamic shared memory
-// render_smem_floats(ll, zz, m) floats.
+// grid (xx, ceil(yy / kRenderTileY)), a multiple of 32 threads; dynamic
+// shared memory render_smem_floats(ll, zz, m) floats.
 __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a) {
   extern __shared__ __align__(16) float rsm[];
   const int x = blockIdx.x, y0 = blockIdx.y * kRenderTileY;
   const int ny = min(kRenderTileY, a.yy - y0);
-  const int LZ = a.ll * a.zz, TL = kRenderTileY * a.ll;
-  float* frac = rsm;                                   // [3][ll][zz]
-  float* mid = frac + 3 * LZ;                          // [3][ll][zz]
-  int* owner = reinterpret_cast<int*>(mid + 3 * LZ);   // [3][zz]
-  WindowStats* st = reinterpret_cast<WindowStats*>(owner + 3 * a.zz);  // [3][TY][ll]
-  float* ival = reinterpret_cast<float*>(st + 3 * TL);  // [3][TY][ll]
-  int* yfin = reinterpret_cast<int*>(ival + 3 * TL);   // [3][TY]
-  float* pf = reinterpret_cast<float*>(yfin + 3 * kRenderTileY);
-  const int pc = render_patch_cols(a.m);
-  const int np = render_patch_rows(a.m) * pc;
-  float* pinv = pf + np;
-  float* u = pinv + np;                                // [2m]
-  for (int t = threadIdx.x; t < 3 * a.zz; t += blockDim.x) {
-    const int c = t / a.zz, z = t - c * a.zz;
-    for (int l = 0; l < a.ll; ++l)
-      render_occupancy(a, c, l, z, &frac[c * LZ + l * a.zz + z],
-                       &mid[c * LZ + l * a.zz + z]);
-    owner[t] = render_owner(a, frac + c * LZ, z);
-  }
-  for (int t = threadIdx.x; t < 3 * kRenderTileY; t += blockDim.x) yfin[t] = 1;
-  for (int t = threadIdx.x; t < 2 * a.m; t += blockDim.x) u[t] = render_u(a, t);
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const RenderSmem s = render_carve(rsm, a.ll, a.zz, a.m);
+  render_phase_setup(a, s, tid, nthr);
+  __syncthreads();
+  render_phase_occupancy(a, s, tid, nthr);
   for (int l = 0; l < a.ll; ++l) {
     __syncthreads();  // the previous layer's windows are done with the patch
-    for (int t = threadIdx.x; t < np; t += blockDim.x)
-      render_stage(a, l, x, y0, ny, t, pf, pinv);
+    if (l == 0) render_phase_cuts(a, s, tid, nthr);
+    render_phase_stage(a, s, l, x, y0, ny, tid, nthr);
     __syncthreads();
-    for (int t = threadIdx.x; t < 3 * ny; t += blockDim.x) {
-      const int c = t / ny, yl = t - c * ny;
-      const int i = (c * kRenderTileY + yl) * a.ll + l;
-      st[i] = render_window(a, c, yl, pf, pinv, pc, u);
-      ival[i] = render_interior(a, c, st[i]);
-      if (!render_finite(st[i])) yfin[c * kRenderTileY + yl] = 0;  // all store 0
-    }
+    render_phase_windows(a, s, l, ny, tid, nthr);
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < 3 * ny * a.zz; t += blockDim.x) {
-    const int c = t / (ny * a.zz);
-    const int r = t - c * ny * a.zz;
-    const int yl = r / a.zz, z = r - yl * a.zz;
-    const int cy = c * kRenderTileY + yl;
-    const int o = yfin[cy] ? owner[c * a.zz + z] : -1;
-    a.out[render_out_index(a, c, x, y0 + yl, z)] =
-        o >= 0 ? ival[cy * a.ll + o]
-               : render_value(a, c, st + cy * a.ll, frac + c * LZ, mid + c * LZ, z);
-  }
+  render_phase_out(a, s, x, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);
 }
 #endif
 
