@@ -492,7 +492,10 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   RingPos p0 = {0, 0u};
   RingPos p1 = next(p0);
   RingPos p2 = next(p1);
-  T* const hbuf[3] = {hn, hn + 3 * RHZ, hn + 6 * RHZ};
+  // New-H buffer (0, 1, 2) of plane x: plane x - 1's is the one before it
+  // and plane x + 1's the one after, cyclically.
+  int hb = 0;
+  auto hbuf = [&](int i) { return hn + (size_t)i * 3 * RHZ; };
 
   // Plane x0: its H phase.
   {
@@ -501,7 +504,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     if (ok && x0 + 1 < X)
       ok = mbar_wait_or_abort(&full[p1.slot], p1.round & 1, sa.status, &abort_flag,
                               sa.wait_cycles);
-    if (ok && doH) h_phase(p0.slot, p1.slot, x0 + 1 < X, hbuf[0], pn);
+    if (ok && doH) h_phase(p0.slot, p1.slot, x0 + 1 < X, hbuf(0), pn);
   }
   // Each iteration: barrier (H of plane x done by every warp), E of plane x,
   // release plane x to the producer, then H of plane x + 1 -- which needs
@@ -509,11 +512,13 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   // buffers keep H(x + 1) off the H(x) and H(x - 1) that E(x) reads.
   for (int x = x0; x < xe; ++x) {
     const int k = x - x0;
+    const int hb1 = hb == 2 ? 0 : hb + 1;  // plane x + 1's buffer
+    const int hb0 = hb == 0 ? 2 : hb - 1;  // plane x - 1's buffer
     compute_sync(ncomp);
     if (abort_flag) break;
     if (x >= xs && doE)
-      e_phase(x, p0.slot, hbuf[k % 3], hbuf[(k + 2) % 3],
-              en + (size_t)(k & 1) * 3 * TYZ, pn + (size_t)(k & 1) * 4 * TY * Pp);
+      e_phase(x, p0.slot, hbuf(hb), hbuf(hb0), en + (size_t)(k & 1) * 3 * TYZ,
+              pn + (size_t)(k & 1) * 4 * TY * Pp);
     // Publish this plane's results to the producer and release its slot.
     fence_async_smem();
     __syncwarp();
@@ -530,9 +535,10 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         ok = mbar_wait_or_abort(&freeb[k1 & 1], (uint32_t)((k1 >> 1) - 1) & 1,
                                 sa.status, &abort_flag, sa.wait_cycles);
       if (ok && doH)
-        h_phase(p1.slot, p2.slot, x + 2 < X, hbuf[k1 % 3],
+        h_phase(p1.slot, p2.slot, x + 2 < X, hbuf(hb1),
                 pn + (size_t)(k1 & 1) * 4 * TY * Pp);
     }
+    hb = hb1;
     p0 = p1;
     p1 = p2;
     p2 = next(p2);
