@@ -64,6 +64,8 @@ def _args():
                   help="c1: skip the batched c4 S-matrix gradient leg")
   ap.add_argument("--no-f16", action="store_true",
                   help="c1: skip the binary16-storage leg")
+  ap.add_argument("--f16-tile-y", type=int, default=-1,
+                  help="c1: tile_y of the binary16 leg (-1: as --tile-y)")
   ap.add_argument("--kernel", type=int, default=0,
                   help="0 auto, 1 register-marching, 2 streamed, 3 lean streamed")
   ap.add_argument("--stages", type=int, default=0)
@@ -416,6 +418,8 @@ def f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells):
   import torch
   from pjz_gb300 import _field
   sp = wl.sim_params._replace(use_reduced_precision=True)
+  if args.f16_tile_y >= 0:
+    sp = sp._replace(launch_params=sp.launch_params._replace(tile_y=args.f16_tile_y))
   kw, omega = _field._setup(eps, src, wl.omega, wl.source_pos, sp)
   plan, prof = _field.phasor_plan(kw, omega)
   run_args = dict(epsilon=eps, absorption_mask=kw["absorption_mask"],

@@ -30,9 +30,13 @@ inline BatchKernel batch_kernel_ptr(int steps) {
 // Lean single-step streamed kernel for (zz, tile_y) and storage (0 FP32,
 // 1 binary16) (kern_lean.cu), or nullptr when no compile-time shape matches.
 StreamKernel lean_kernel_ptr(int zz, int tile_y, int storage);
+// Block size bound of that instantiation (0 when none matches).
+int lean_kernel_threads(int zz, int tile_y, int storage);
+// Tile height of the tall binary16 lean shape for zz, or 0.
+int lean_tall_tile_y(int zz);
 // Lean two-step streamed kernel, likewise (kern_lean2.cu).
 StreamKernel lean2_kernel_ptr(int zz, int tile_y, int storage);
-// Block size bound of the lean kernel.
+// Block size bound of the lean two-step kernel.
 constexpr int kLeanThreads = 384;
 // Permittivity rendering kernel (kern_render.cu).
 using RenderKernel = void (*)(RenderArgs);

@@ -54,7 +54,8 @@ __host__ __device__ inline int lean_warps_pml(int ty, int plo, int phi) {
 // 16-byte boundary, as the bulk copies need.  After the ring: new H
 // [3][3][RH*Z] (planes x - 1, x, x + 1: the E phase of plane x shares its
 // barrier interval with the H phase of plane x + 1), new E [2][3][TY*Z],
-// new PML state [2][4][TY*Pp] (T), then the mbarriers.
+// new PML state [2][4][TY*Pp] (T), the z coefficient table [6][Z] (FP32:
+// 1/kappa and the CPML b, c of E, then of H), then the mbarriers.
 template <typename T>
 struct LeanGeom {
   int TY, Z, Pp, RE, RH, MT;
@@ -77,9 +78,10 @@ struct LeanGeom {
   __host__ __device__ size_t hn_bytes() const { return 3 * 3 * (size_t)RH * Z * sizeof(T); }
   __host__ __device__ size_t en_bytes() const { return 2 * 3 * (size_t)TY * Z * sizeof(T); }
   __host__ __device__ size_t pn_bytes() const { return 2 * 4 * (size_t)TY * Pp * sizeof(T); }
+  __host__ __device__ size_t zc_bytes() const { return 6 * (size_t)Z * sizeof(float); }
   __host__ __device__ size_t bytes(int stages) const {
     return (size_t)stages * stage + hn_bytes() + en_bytes() + pn_bytes() +
-           (size_t)(2 * stages + 2) * sizeof(uint64_t) + 16;
+           zc_bytes() + (size_t)(2 * stages + 2) * sizeof(uint64_t) + 16;
   }
 };
 
@@ -148,7 +150,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   T* hn = reinterpret_cast<T*>(sm + (size_t)S * g.stage);  // [3][3][RH*Z]
   T* en = hn + 3 * 3 * RHZ;                                // [2][3][TY*Z]
   T* pn = en + 2 * 3 * TYZ;                                // [2][4][TY*Pp]
-  uint64_t* full = reinterpret_cast<uint64_t*>(pn + 2 * 4 * TY * Pp);
+  float* zcs = reinterpret_cast<float*>(pn + 2 * 4 * TY * Pp);  // [6][Z]
+  uint64_t* full = reinterpret_cast<uint64_t*>(zcs + 6 * Z);
   uint64_t* done = full + S;
   uint64_t* freeb = done + S;
   __shared__ int abort_flag;
@@ -193,6 +196,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     const size_t nw = ((size_t)S * g.stage + g.hn_bytes() + g.en_bytes() +
                        g.pn_bytes()) / 4;
     for (size_t i = tid; i < nw; i += blockDim.x) w[i] = 0u;
+    for (int i = tid; i < 6 * Z; i += blockDim.x) zcs[i] = a.zc[i];
   }
   fence_async_smem();
   __syncthreads();
@@ -304,17 +308,10 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const bool zhi = z0 + 4 < Z;  // a z + 1 neighbour inside the domain
   const bool zlo = z0 > 0;      // a z - 1 neighbour inside the domain
 
-  float ike[4], ikh[4], be[4], ce[4], bh[4], ch[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const int z = min(z0 + k, Z - 1);  // idle lanes read a valid entry
-    ike[k] = a.zc[z];
-    ikh[k] = a.zc[3 * Z + z];
-    be[k] = pml ? a.zc[Z + z] : 0.f;
-    ce[k] = pml ? a.zc[2 * Z + z] : 0.f;
-    bh[k] = pml ? a.zc[4 * Z + z] : 0.f;
-    ch[k] = pml ? a.zc[5 * Z + z] : 0.f;
-  }
+  // z coefficients of the quad (z0 + 3 < Z for every item, idle or not)
+  // are read from the shared table in each phase rather than held in 24
+  // registers across the plane loop.
+  const float* zq = zcs + z0;
   const float mdt = -a.dt;
   // Source box rows and z range of this item (the plane test is separate).
   const bool src_row = a.snc > 0 && yE >= a.sy0 && yE < a.sy0 + a.sny &&
@@ -354,10 +351,13 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) Q::ld(Hs + c * RHZ + ieH, ho[c]);
-      float pa[4], pb[4];
+      float pa[4], pb[4], ikh[4], bh[4], ch[4];
+      Quad<float>::ld(zq + 3 * Z, ikh);
       if (pml) {
         Q::ld(Ps + pH, pa);
         Q::ld(Ps + RH * Pp + pH, pb);
+        Quad<float>::ld(zq + 4 * Z, bh);
+        Quad<float>::ld(zq + 5 * Z, ch);
       }
       float hx[4], hy[4], hz[4];
 #pragma unroll
@@ -420,10 +420,13 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         Q::ld(Cs + c * TYZ + icE, cb[c]);
       }
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
-      float pa[4], pb[4];
+      float pa[4], pb[4], ike[4], be[4], ce[4];
+      Quad<float>::ld(zq, ike);
       if (pml) {
         Q::ld(Ps + 2 * RH * Pp + pE, pa);
         Q::ld(Ps + 3 * RH * Pp + pE, pb);
+        Quad<float>::ld(zq + Z, be);
+        Quad<float>::ld(zq + 2 * Z, ce);
       }
       const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
       float enew[3][4];
@@ -548,18 +551,27 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 // (zz, tile_y) shapes of the lean kernel: the streamed kernel's tile heights
 // for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
 #define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
+// Taller binary16 tiles (half the shared memory per row): 16 warps per CTA
+// hide more latency than 9 and the y halo is half as large per cell.
+#define PJZ_LEAN_SHAPES_F16(X_) X_(64, 28)
 
-// Block bound of a lean kernel instantiation (one CTA per SM: the ring and
-// staging buffers take most of the shared memory; two binary16 CTAs per SM
-// measured slower, their registers capped at 96 with spills).
-template <typename T>
+// Block bound of a lean kernel instantiation: one CTA per SM (the ring and
+// staging buffers take most of the shared memory), 12 warps, or 16 for the
+// tall binary16 tiles (whose registers are capped at 128 by that).
+constexpr bool lean_tall_shape(int zc, int tyc) {
+#define PJZ_IS_TALL(ZC, TYC) (zc == ZC && tyc == TYC) ||
+  return PJZ_LEAN_SHAPES_F16(PJZ_IS_TALL) false;
+#undef PJZ_IS_TALL
+}
+template <int ZC, int TYC, typename T>
 struct LeanBounds {
-  static constexpr int threads = 384;
+  static constexpr int threads = sizeof(T) == 2 && lean_tall_shape(ZC, TYC) ? 512 : 384;
   static constexpr int blocks = 1;
 };
 
 template <int ZC, int TYC, typename T>
-__global__ void __launch_bounds__(LeanBounds<T>::threads, LeanBounds<T>::blocks)
+__global__ void __launch_bounds__(LeanBounds<ZC, TYC, T>::threads,
+                                  LeanBounds<ZC, TYC, T>::blocks)
     yee_lean_kernel(const StreamArgs sa) {
   extern __shared__ __align__(16) unsigned char lean_sm[];
   lean_tile<ZC, TYC, T>(sa, blockIdx.x, blockIdx.y, lean_sm);

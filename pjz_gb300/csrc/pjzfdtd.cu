@@ -292,6 +292,8 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
 
 // Whether auto selection takes the lean kernel where it applies.
 constexpr bool kLeanAuto = false;
+// Whether auto selection takes the tall binary16 lean tile where it applies.
+constexpr bool kLeanTallAuto = false;
 
 // Lean streamed kernel (lean_kernel.cuh) on top of a resolved streamed
 // plan: a compile-time (zz, tile_y) shape, one step per launch, z-PML slab
@@ -316,8 +318,7 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
   }
   const int warps = lean_warps_interior(Z, ty, p.pml_lo, p.pml_hi) +
                     lean_warps_pml(ty, p.pml_lo, p.pml_hi);
-  const int bound = p.storage == PJZFDTD_STORAGE_F16 ? LeanBounds<__half>::threads
-                                                     : LeanBounds<float>::threads;
+  const int bound = lean_kernel_threads(Z, ty, p.storage);
   if (warps * 32 + 32 > bound)
     return required ? fail(PJZFDTD_ERR_UNSUPPORTED, "lean tile needs %d warps",
                            warps)
@@ -383,6 +384,23 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
     if (Z % 4 != 0 || Z > zmax)
       return fail(PJZFDTD_ERR_UNSUPPORTED,
                   "binary16 storage needs the lean kernel (zz %% 4 == 0)");
+    // The tall binary16 tile (one step per launch): resolved like the
+    // streamed plan at the automatic height, then given the tall height.
+    const int tall = pl->p.storage == PJZFDTD_STORAGE_F16 && pl->p.steps_per_pass != 2
+                         ? lean_tall_tile_y(Z)
+                         : 0;
+    const bool asked = tall > 0 && pl->p.tile_y == tall;
+    if (asked || (tall > 0 && pl->p.tile_y == 0 && kLeanTallAuto)) {
+      const int req_ty = pl->p.tile_y;
+      pl->p.tile_y = 0;
+      int32_t rc = resolve_stream(pl);
+      pl->p.tile_y = req_ty;
+      if (rc) return rc;
+      pl->tile_y = tall;
+      if ((rc = resolve_lean(pl, asked))) return rc;
+      if (pl->kernel == 3) return PJZFDTD_OK;
+      pl->seg_x = 0;  // not applicable: the plan below starts over
+    }
     int32_t rc = resolve_stream(pl);
     if (rc) return rc;
     if ((rc = resolve_lean(pl, true))) return rc;

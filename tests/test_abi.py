@@ -182,3 +182,24 @@ def test_binary16_plans_stay_out_of_batches(lib):
             pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)))
   with pytest.raises(NotImplementedError, match="binary16"):
     engine.Batch([engine.Plan(**kw, storage=engine.STORAGE_F16)])
+
+
+@pytest.mark.parametrize("pml,ok", [((0, 0), True), ((8, 8), True), ((4, 12), True),
+                                    ((12, 12), False)])
+def test_tall_binary16_tile(lib, pml, ok):
+  """tile_y=28 at zz 64 with binary16 storage takes the tall lean tile (16
+  warps at most: z-PML slabs up to 16 cells wide); wider slabs need more
+  warps than its block bound and are refused.  FP32 has no such tile."""
+  Z = 64
+  kw = dict(domain=(20, 61, Z), offset=(0, 0, 0), region=(20, 61, Z), tt=20,
+            dt=0.5, pml_widths=pml, pml_kappa=np.ones((Z, 2)),
+            pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)), tile_y=28)
+  if not ok:
+    with pytest.raises(NotImplementedError, match="warps"):
+      engine.Plan(**kw, storage=engine.STORAGE_F16)
+    return
+  cfg = engine.Plan(**kw, storage=engine.STORAGE_F16).launch_config()
+  assert cfg["kernel"] == 3 and cfg["tile_y"] == 28
+  assert cfg["threads"] <= 512 and cfg["threads"] % 32 == 0
+  with pytest.raises(ValueError, match="exceeds shared"):
+    engine.Plan(**kw)

@@ -39,6 +39,37 @@ def test_f16_snapshots_bit_exact(native, Z, TY, pml, src):
   assert np.array_equal(got, want), np.abs(got - want).max()
 
 
+@pytest.mark.parametrize("pml", [(8, 8), (0, 0), (4, 12)])
+@pytest.mark.parametrize("src", ["x", "y", "z"])
+@pytest.mark.parametrize("stages,seg_x", [(0, 6), (3, 19), (2, 4)])
+def test_f16_tall_tile_bit_exact(native, pml, src, stages, seg_x):
+  """The tall binary16 tile (zz 64, tile_y 28, up to 16 warps) with a
+  ragged last tile, over ring depths and segments."""
+  case = random_problem(hash((pml, src, stages, 28)) % 1000, X=19, Y=61, Z=64,
+                        pml=pml, src=src, src_pos=5 if src == "z" else 7,
+                        tt=24, steps=(9, 24, 4))
+  want = oracle.run(**oracle_kwargs(case), storage="f16")["out"]
+  got, _, _ = gpu16(case, tile_y=28, stages=stages, seg_x=seg_x)
+  assert np.array_equal(got, want), np.abs(got - want).max()
+
+
+def test_f16_tall_tile_phasors_state_and_chaining(native):
+  case = random_problem(52, X=17, Y=70, Z=64, pml=(8, 8), tt=40, steps=(10, 40, 3))
+  ns = len(range(*case["output_steps"]))
+  w = np.random.default_rng(7).normal(size=(6, ns)).astype(np.float32)
+  f0 = np.random.default_rng(8).normal(size=(6,) + case["domain"]).astype(np.float32)
+  want = oracle.run(**oracle_kwargs(case), mode="project", weights=w, record_h=True,
+                    fields=f0.copy(), storage="f16")
+  got, got_h, got_f = gpu16(case, out_mode=engine.OUT_PHASORS, weights=w,
+                            record_h=True, fields=f0.copy(), tile_y=28)
+  assert np.array_equal(got, want["out"])
+  assert np.array_equal(got_h, want["out_h"])
+  assert np.array_equal(got_f, want["fields"])
+  snap = oracle.run(**oracle_kwargs(case), storage="f16")["out"]
+  got, _, _ = gpu16(case, split=17, tile_y=28)
+  assert np.array_equal(got, snap)
+
+
 def test_f16_phasors_record_h_state_and_chaining(native):
   case = random_problem(51, X=17, Y=30, Z=64, pml=(8, 8), tt=40, steps=(10, 40, 3))
   ns = len(range(*case["output_steps"]))

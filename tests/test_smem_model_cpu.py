@@ -379,8 +379,9 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
   s_off = p_off + 4 * RH * Pp
 
   def smem_bytes(sw):
+    # `esz` bytes per value (the absorber's FP32 windows are few).
     floats = S * (s_off + sw) + hbuf * 3 * RH * Z + 2 * 3 * TY * Z + 2 * 4 * TY * Pp
-    return floats * 4 + (2 * S + 2) * 8 + 16
+    return floats * esz + (2 * S + 2) * 8 + 16
 
   if smem_bytes(0) > SMEM_BUDGET:
     return None
@@ -1075,8 +1076,11 @@ def test_random_shapes():
 # The lean kernel's new-H buffers and barriers per plane.
 LEAN_PROTOCOL = dict(hbuf=3, barriers=1)
 
+# Tall tiles of the binary16 lean kernel (PJZ_LEAN_SHAPES_F16).
+LEAN_F16_ONLY = {(64, 28)}
+
 LEAN_CASES = [(5, 30, 64, 14), (4, 41, 48, 19), (3, 61, 32, 29), (6, 9, 16, 5),
-              (4, 13, 24, 3)]
+              (4, 13, 24, 3), (3, 61, 64, 28)]
 
 
 @pytest.mark.parametrize("esz", [4, 2])
@@ -1090,6 +1094,8 @@ def test_lean_compute_accesses(X, Y, Z, TY, plo, phi, esz):
   each update needs, race-free between barriers, every row stored once."""
   if plo + phi > Z:
     pytest.skip("slabs wider than the domain")
+  if (Z, TY) in LEAN_F16_ONLY and esz != 2:
+    pytest.skip("a binary16-only shape")
   checked = 0
   for S, seg_x in itertools.product((2, 3, 4), (2, X)):
     res = one_step(X, Y, Z, plo, phi, TY, S, seg_x, min_ncomp(Z), None, lean=True,
