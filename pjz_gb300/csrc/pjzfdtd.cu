@@ -1376,9 +1376,22 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
                 xx, yy, zz, magnification);
   if (ll > 1 && !interface_positions)
     return fail(PJZFDTD_ERR_INVALID, "%d interface positions needed", ll - 1);
-  const size_t smem = render_smem_floats(ll, zz, magnification) * sizeof(float);
+  // Layers staged together: all of them while the CTA stays within 48 KB
+  // of shared memory (several CTAs per SM), else fewer, down to one; the
+  // patches' flat indices must keep t * columns below 2^32 (render_div).
+  const int prow = render_patch_rows(magnification);
+  const int pcol = render_patch_cols(magnification);
+  auto bytes = [&](int g) {
+    return render_smem_floats(ll, zz, magnification, g) * sizeof(float);
+  };
+  auto exact = [&](int g) {
+    return (uint64_t)g * prow * pcol * (uint64_t)pcol < ((uint64_t)1 << 32);
+  };
+  int group = ll;
+  while (group > 1 && (bytes(group) > 48 * 1024 || !exact(group))) --group;
+  const size_t smem = bytes(group);
   const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
-  if (smem > kSmemMax || yblocks > 65535)
+  if (smem > kSmemMax || !exact(group) || yblocks > 65535)
     return fail(PJZFDTD_ERR_INVALID,
                 "zz = %d with %d layers at magnification %d (or yy = %d) "
                 "exceeds one CTA's reach", zz, ll, magnification, yy);
@@ -1391,6 +1404,9 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   a.zz = zz;
   a.m = magnification;
   a.simple = use_simple_averaging != 0;
+  a.group = group;
+  a.col_magic = render_col_magic((uint32_t)pcol);
+  a.row_magic = render_col_magic((uint32_t)prow);
   for (int i = 0; i + 1 < ll; ++i) a.pos[i] = interface_positions[i];
   const RenderKernel k = render_kernel_ptr();
   if (smem > 48 * 1024)

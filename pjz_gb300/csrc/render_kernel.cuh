@@ -19,12 +19,13 @@
 // (subpixel smoothing, diagonal of the interface projection only).
 //
 // One CTA per (x, block of kRenderTileY y cells), all three components.
-// It tabulates the z occupancy of each component's cells, then, one layer
-// at a time, stages the layer's pixel patch that the block's windows cover
-// (3m rows x (2m*ny + m) columns, edge pixels repeated) in shared memory
-// with each pixel's reciprocal computed once, computes every window's
-// statistics from the patch, and finally writes the (component, y, z)
-// outputs with z fastest, coalesced.  A z cell that lies wholly inside one
+// It tabulates the z occupancy of each component's cells, then, a group of
+// layers at a time (as many as the host fits in shared memory), stages the
+// layers' pixel patches that the block's windows cover (3m rows x
+// (2m*ny + m) columns each, edge pixels repeated) with each pixel's
+// reciprocal computed once, computes every window's statistics from the
+// patches, and finally writes the (component, y, z) outputs with z fastest,
+// coalesced.  A z cell that lies wholly inside one
 // layer (its fraction exactly 1, all others exactly 0) has the same value at
 // every such z of a column: it is computed once per (y, layer) and copied,
 // and only the cells an interface cuts take the full mix.  Both give the
@@ -42,6 +43,7 @@
 
 #include <math.h>
 #include <stddef.h>
+#include <stdint.h>
 
 #ifdef __CUDACC__
 #define PJZ_HD __host__ __device__ __forceinline__
@@ -58,6 +60,9 @@ struct RenderArgs {
   const float* layers;  // (ll, 2m*xx, 2m*yy)
   float* out;           // (3, xx, yy, zz)
   int ll, xx, yy, zz, m, simple;
+  int group;            // layers staged together (1 .. ll)
+  uint32_t col_magic;   // render_col_magic(patch columns)
+  uint32_t row_magic;   // render_col_magic(patch rows)
   float pos[kRenderMaxLayers - 1];  // interface positions, increasing
 };
 
@@ -88,18 +93,28 @@ PJZ_HD int render_imax(int a, int b) { return a > b ? a : b; }
 PJZ_HD int render_patch_rows(int m) { return 3 * m; }
 PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
 
-// Shared-memory floats of one CTA: occupancy frac / mid [3][ll][zz], the
-// layer that fills each z cell [3][zz] (int, -1 when an interface cuts it),
-// window statistics [3][kRenderTileY][ll] of 4 floats, one-layer values
-// [3][kRenderTileY][ll], per (component, y) whether every layer's statistics
-// are finite [3][kRenderTileY] (int), the pixel patch and its reciprocals
-// [2][3m][2m*kRenderTileY + m], the pixel offsets u [2m], the interface
-// positions [kRenderMaxLayers], and per component the z cells an interface
-// cuts [3][zz] (int) and their count [4] (int).
-PJZ_HD size_t render_smem_floats(int ll, int zz, int m) {
+// t / d for the patches' flat indices: floor(t * ceil(2^32 / d) / 2^32)
+// equals floor(t / d) while t * d < 2^32, which the host's limits keep.
+PJZ_HD uint32_t render_col_magic(uint32_t d) {
+  return (uint32_t)((((uint64_t)1 << 32) + d - 1) / d);
+}
+PJZ_HD int render_div(int t, uint32_t magic) {
+  return (int)(((uint64_t)(uint32_t)t * magic) >> 32);
+}
+
+// Shared-memory floats of one CTA staging `group` layers at once: occupancy
+// frac / mid [3][ll][zz], the layer that fills each z cell [3][zz] (int, -1
+// when an interface cuts it), window statistics [3][kRenderTileY][ll] of 4
+// floats, one-layer values [3][kRenderTileY][ll], per (component, y)
+// whether every layer's statistics are finite [3][kRenderTileY] (int), the
+// pixel patches and their reciprocals [2][group][3m][2m*kRenderTileY + m],
+// the pixel offsets u [2m], the interface positions [kRenderMaxLayers], and
+// per component the z cells an interface cuts [3][zz] (int) and their
+// count [4] (int).
+PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group) {
   return 6 * (size_t)ll * zz + 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
          3 * kRenderTileY +
-         2 * (size_t)render_patch_rows(m) * render_patch_cols(m) + 2 * m +
+         2 * (size_t)group * render_patch_rows(m) * render_patch_cols(m) + 2 * m +
          kRenderMaxLayers + 3 * (size_t)zz + 4;
 }
 
@@ -111,8 +126,8 @@ struct RenderSmem {
   WindowStats* st;  // [3][kRenderTileY][ll]
   float* ival;      // [3][kRenderTileY][ll]
   int* yfin;        // [3][kRenderTileY]
-  float* pf;        // [3m][pc]
-  float* pinv;      // [3m][pc]
+  float* pf;        // [group][3m][pc]
+  float* pinv;      // [group][3m][pc]
   float* u;         // [2m]
   float* pos;       // [kRenderMaxLayers]
   int* cut;         // [3][zz]: z cells no single layer fills
@@ -120,9 +135,9 @@ struct RenderSmem {
   float* end;
 };
 
-PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m) {
+PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m, int group) {
   const int LZ = ll * zz, TL = kRenderTileY * ll;
-  const int np = render_patch_rows(m) * render_patch_cols(m);
+  const int np = group * render_patch_rows(m) * render_patch_cols(m);
   RenderSmem s;
   s.frac = sm;
   s.mid = s.frac + 3 * LZ;
@@ -192,20 +207,6 @@ PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
   w.gx = 12.0f * sxu / n;
   w.gy = 12.0f * syu / n;
   return w;
-}
-
-// Stages row r, column cc of the patch of layer `l` for the CTA at (x, y0):
-// the pixel and its reciprocal.
-PJZ_HD void render_stage(const RenderArgs& a, int l, int x, int y0, int r, int cc,
-                         float* pf, float* pinv) {
-  const int k = 2 * a.m, pc = render_patch_cols(a.m);
-  const int PX = k * a.xx, PY = k * a.yy;
-  const int px = render_imax(k * x - a.m + r, 0);
-  const int py = render_imax(k * y0 - a.m + cc, 0);
-  const float* L = a.layers + (size_t)l * PX * PY;
-  const float f = render_load(L, (size_t)px * PY + py);
-  pf[r * pc + cc] = f;
-  pinv[r * pc + cc] = 1.0f / f;
 }
 
 // The value from the fraction-weighted sums over the layers.
@@ -283,10 +284,28 @@ PJZ_HD void render_phase_occupancy(const RenderArgs& a, const RenderSmem& s,
     }
 }
 
-// Phase 3 (beside the first layer's phase 4, after a barrier that follows
+// Phase 3 (beside the first group's staging, after a barrier that follows
 // phase 2): per component, the z cells no single layer fills, in increasing
-// z, one thread per component.
-PJZ_HD void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
+// z.  On the device warp c (c < 3) compacts component c with ballots; the
+// host walks z in order, which gives the same list.
+#if defined(__CUDA_ARCH__)
+__device__ __forceinline__ void render_phase_cuts(const RenderArgs& a,
+                                                  const RenderSmem& s, int tid,
+                                                  int nthr) {
+  const int c = tid >> 5, lane = tid & 31;
+  if (c >= 3) return;
+  int n = 0;
+  for (int z0 = 0; z0 < a.zz; z0 += 32) {
+    const int z = z0 + lane;
+    const bool f = z < a.zz && s.owner[c * a.zz + z] < 0;
+    const unsigned m = __ballot_sync(0xffffffffu, f);
+    if (f) s.cut[c * a.zz + n + __popc(m & ((1u << lane) - 1u))] = z;
+    n += __popc(m);
+  }
+  if (lane == 0) s.ncut[c] = n;
+}
+#else
+inline void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
                               int nthr) {
   for (int c = tid; c < 3; c += nthr) {
     int n = 0;
@@ -295,27 +314,47 @@ PJZ_HD void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
     s.ncut[c] = n;
   }
 }
+#endif
 
-// Phase 4, per layer: the pixel patch of the CTA at (x, y0) with ny tile
-// rows (the columns its windows cover: 2m*ny + m).
-PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l,
-                               int x, int y0, int ny, int tid, int nthr) {
-  const int cols = 2 * a.m * ny + a.m;
-  for (int r = 0; r < render_patch_rows(a.m); ++r)
-    for (int cc = tid; cc < cols; cc += nthr)
-      render_stage(a, l, x, y0, r, cc, s.pf, s.pinv);
+// Phase 4, per group of layers l0 .. l0 + ng - 1: their pixel patches for
+// the CTA at (x, y0) with ny tile rows (the columns its windows cover:
+// 2m*ny + m), one flat index over (layer, row, column).
+PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
+                               int ng, int x, int y0, int ny, int tid, int nthr) {
+  const int k = 2 * a.m, pc = render_patch_cols(a.m);
+  const int cols = k * ny + a.m, rows = ng * render_patch_rows(a.m);
+  const int PX = k * a.xx, PY = k * a.yy;
+  for (int t = tid; t < rows * pc; t += nthr) {
+    const int gr = render_div(t, a.col_magic);  // (layer, row) of the group
+    const int cc = t - gr * pc;
+    if (cc >= cols) continue;
+    const int g = render_div(gr, a.row_magic);  // layer of the group
+    const int r = gr - g * render_patch_rows(a.m);
+    const int px = render_imax(k * x - a.m + r, 0);
+    const int py = render_imax(k * y0 - a.m + cc, 0);
+    const float* L = a.layers + (size_t)(l0 + g) * PX * PY;
+    const float f = render_load(L, (size_t)px * PY + py);
+    s.pf[t] = f;
+    s.pinv[t] = 1.0f / f;
+  }
 }
 
-// Phase 5, per layer: window statistics and one-layer values of the
-// (component, row) windows of the staged patch.
-PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l,
-                                 int ny, int tid, int nthr) {
+// Phase 5, per group: window statistics and one-layer values of the
+// (component, row, layer) windows of the staged patches.
+PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l0,
+                                 int ng, int ny, int tid, int nthr) {
   const int pc = render_patch_cols(a.m);
-  for (int t = tid; t < 3 * ny; t += nthr) {
-    const int c = t >= 2 * ny ? 2 : (t >= ny ? 1 : 0), yl = t - c * ny;
+  const int np1 = render_patch_rows(a.m) * pc;  // one layer's patch
+  for (int t = tid; t < 3 * ny * ng; t += nthr) {
+    int g = 0, r = t;
+    while (r >= 3 * ny) {  // ng is small: at most kRenderMaxLayers
+      r -= 3 * ny;
+      ++g;
+    }
+    const int c = r >= 2 * ny ? 2 : (r >= ny ? 1 : 0), yl = r - c * ny;
     const int cy = c * kRenderTileY + yl;
-    const int i = cy * a.ll + l;
-    s.st[i] = render_window(a, c, yl, s.pf, s.pinv, pc, s.u);
+    const int i = cy * a.ll + l0 + g;
+    s.st[i] = render_window(a, c, yl, s.pf + g * np1, s.pinv + g * np1, pc, s.u);
     s.ival[i] = render_interior(a, c, s.st[i]);
     if (!render_finite(s.st[i])) s.yfin[cy] = 0;  // any writer stores 0
   }
@@ -358,23 +397,24 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
 }
 
 #if defined(__CUDACC__) && defined(PJZ_RENDER_KERNEL)  // kern_render.cu only
-// grid (xx, ceil(yy / kRenderTileY)), a multiple of 32 threads; dynamic
-// shared memory render_smem_floats(ll, zz, m) floats.
+// grid (xx, ceil(yy / kRenderTileY)), a multiple of 32 threads (at least
+// 96); dynamic shared memory render_smem_floats(ll, zz, m, group) floats.
 __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a) {
   extern __shared__ __align__(16) float rsm[];
   const int x = blockIdx.x, y0 = blockIdx.y * kRenderTileY;
   const int ny = min(kRenderTileY, a.yy - y0);
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const RenderSmem s = render_carve(rsm, a.ll, a.zz, a.m);
+  const RenderSmem s = render_carve(rsm, a.ll, a.zz, a.m, a.group);
   render_phase_setup(a, s, tid, nthr);
   __syncthreads();
   render_phase_occupancy(a, s, tid, nthr);
-  for (int l = 0; l < a.ll; ++l) {
-    __syncthreads();  // the previous layer's windows are done with the patch
-    if (l == 0) render_phase_cuts(a, s, tid, nthr);
-    render_phase_stage(a, s, l, x, y0, ny, tid, nthr);
+  for (int l0 = 0; l0 < a.ll; l0 += a.group) {
+    const int ng = min(a.group, a.ll - l0);
+    __syncthreads();  // the previous group's windows are done with the patches
+    if (l0 == 0) render_phase_cuts(a, s, tid, nthr);
+    render_phase_stage(a, s, l0, ng, x, y0, ny, tid, nthr);
     __syncthreads();
-    render_phase_windows(a, s, l, ny, tid, nthr);
+    render_phase_windows(a, s, l0, ng, ny, tid, nthr);
   }
   __syncthreads();
   render_phase_out(a, s, x, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);

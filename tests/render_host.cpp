@@ -26,9 +26,11 @@ constexpr size_t kGuard = 4096;
 constexpr uint32_t kSentinel = 0x7fc0dead;  // a NaN no output takes
 }  // namespace
 
-// Returns 0, or 1 when a read or write left its array.
+// Stages `group` layers at a time (0: all).  Returns 0, or 1 when a read or
+// write left its array.
 extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
-                           int m, const float* pos, int simple, float* out) {
+                           int m, const float* pos, int simple, int group,
+                           float* out) {
   const size_t out_floats = (size_t)3 * xx * yy * zz;
   std::vector<float> guarded(out_floats + 2 * kGuard);
   for (float& v : guarded) memcpy(&v, &kSentinel, 4);
@@ -41,11 +43,14 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   a.zz = zz;
   a.m = m;
   a.simple = simple != 0;
+  a.group = group > 0 && group < ll ? group : ll;
+  a.col_magic = render_col_magic((uint32_t)render_patch_cols(m));
+  a.row_magic = render_col_magic((uint32_t)render_patch_rows(m));
   for (int i = 0; i + 1 < ll; ++i) a.pos[i] = pos[i];
   g_render_layer_floats = (size_t)(2 * m * xx) * (2 * m * yy);
   g_render_bad = 0;
-  std::vector<float> sm(render_smem_floats(ll, zz, m));
-  const RenderSmem s = render_carve(sm.data(), ll, zz, m);
+  std::vector<float> sm(render_smem_floats(ll, zz, m, a.group));
+  const RenderSmem s = render_carve(sm.data(), ll, zz, m, a.group);
   if (s.end != sm.data() + sm.size()) return 1;  // carving
   for (int x = 0; x < xx; ++x)
     for (int y0 = 0; y0 < yy; y0 += kRenderTileY) {
@@ -53,11 +58,12 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
       for (int t = 0; t < kThreads; ++t) render_phase_setup(a, s, t, kThreads);
       for (int t = 0; t < kThreads; ++t) render_phase_occupancy(a, s, t, kThreads);
       for (int t = 0; t < kThreads; ++t) render_phase_cuts(a, s, t, kThreads);
-      for (int l = 0; l < ll; ++l) {
+      for (int l0 = 0; l0 < ll; l0 += a.group) {
+        const int ng = a.group < ll - l0 ? a.group : ll - l0;
         for (int t = 0; t < kThreads; ++t)
-          render_phase_stage(a, s, l, x, y0, ny, t, kThreads);
+          render_phase_stage(a, s, l0, ng, x, y0, ny, t, kThreads);
         for (int t = 0; t < kThreads; ++t)
-          render_phase_windows(a, s, l, ny, t, kThreads);
+          render_phase_windows(a, s, l0, ng, ny, t, kThreads);
       }
       for (int t = 0; t < kThreads; ++t)
         render_phase_out(a, s, x, y0, ny, t >> 5, kThreads >> 5, t & 31, a.out);

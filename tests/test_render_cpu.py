@@ -32,12 +32,12 @@ def host(tmp_path_factory):
   h = ctypes.CDLL(lib)
   P = ctypes.c_void_p
   I = ctypes.c_int
-  h.render_host.argtypes = [P, I, I, I, I, I, P, I, P]
+  h.render_host.argtypes = [P, I, I, I, I, I, P, I, I, P]
   h.render_host.restype = I
   return h
 
 
-def render(host, layers, pos, m, zz, simple=False, finite=True):
+def render(host, layers, pos, m, zz, simple=False, finite=True, group=0):
   layers = np.ascontiguousarray(layers, np.float32)
   ll, px, py = layers.shape
   xx, yy = px // (2 * m), py // (2 * m)
@@ -45,7 +45,7 @@ def render(host, layers, pos, m, zz, simple=False, finite=True):
   out = np.full((3, xx, yy, zz), np.nan, np.float32)
   bad = host.render_host(layers.ctypes.data, ll, xx, yy, zz, m,
                          pos.ctypes.data if pos.size else None, int(simple),
-                         out.ctypes.data)
+                         group, out.ctypes.data)
   assert bad == 0, "a read or write left its array"
   if finite:
     assert np.isfinite(out).all(), "an output was not written"
@@ -70,6 +70,19 @@ def test_matches_fp64_oracle(host, ll, xx, yy, zz, m, simple):
   want = eo.epsilon(layers.astype(np.float32).astype(np.float64),
                     pos.astype(np.float32).astype(np.float64), m, zz, simple)
   np.testing.assert_allclose(got, want, rtol=2e-5, atol=0)
+
+
+@pytest.mark.parametrize("ll,m", [(5, 2), (16, 1), (3, 3)])
+def test_layer_groups_give_the_same_floats(host, ll, m):
+  """Staging the layers in groups of any size (the library stages as many
+  as fit its shared-memory budget) changes no output bit."""
+  rng = np.random.default_rng(ll * 10 + m)
+  xx, yy, zz = 3, 37, 11
+  layers = rng.uniform(1.0, 12.25, (ll, 2 * m * xx, 2 * m * yy))
+  pos = np.sort(rng.uniform(-1.0, zz + 1.0, ll - 1))
+  want = render(host, layers, pos, m, zz)
+  for g in range(1, ll):
+    np.testing.assert_array_equal(render(host, layers, pos, m, zz, group=g), want)
 
 
 def test_reference_layer_tables(host):
