@@ -130,6 +130,27 @@ struct Quad<__half> {
   }
 };
 
+// (zz, tile_y) shapes of the lean kernel: the streamed kernel's tile heights
+// for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
+#define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
+// Taller binary16 tiles (half the shared memory per row): 16 warps per CTA
+// hide more latency than 9 and the y halo is half as large per cell.
+#define PJZ_LEAN_SHAPES_F16(X_) X_(64, 28)
+
+// Block bound of a lean kernel instantiation: one CTA per SM (the ring and
+// staging buffers take most of the shared memory), 12 warps, or 16 for the
+// tall binary16 tiles (whose registers are capped at 128 by that).
+constexpr bool lean_tall_shape(int zc, int tyc) {
+#define PJZ_IS_TALL(ZC, TYC) (zc == ZC && tyc == TYC) ||
+  return PJZ_LEAN_SHAPES_F16(PJZ_IS_TALL) false;
+#undef PJZ_IS_TALL
+}
+template <int ZC, int TYC, typename T>
+struct LeanBounds {
+  static constexpr int threads = sizeof(T) == 2 && lean_tall_shape(ZC, TYC) ? 512 : 384;
+  static constexpr int blocks = 1;
+};
+
 // One CTA of the lean kernel: tile `tile` of y rows, segment `seg` of x
 // planes.  ZC / TYC: zz and tile_y (compile-time); T: storage type of the
 // fields, coefficients and z-PML state in HBM and shared memory (float, or
@@ -308,10 +329,26 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const bool zhi = z0 + 4 < Z;  // a z + 1 neighbour inside the domain
   const bool zlo = z0 > 0;      // a z - 1 neighbour inside the domain
 
-  // z coefficients of the quad (z0 + 3 < Z for every item, idle or not)
-  // are read from the shared table in each phase rather than held in 24
-  // registers across the plane loop.
+  // z coefficients of the quad (z0 + 3 < Z for every item, idle or not):
+  // 1/kappa, b, c of E then of H.
   const float* zq = zcs + z0;
+  // Register-capped shapes read them from the table; the others hold them.
+  constexpr bool kZcShared = LeanBounds<ZC, TYC, T>::threads > 384;
+  float rz[6][4];
+  if constexpr (!kZcShared) {
+#pragma unroll
+    for (int r = 0; r < 6; ++r)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) rz[r][j] = a.zc[r * Z + z0 + j];
+  }
+  auto zload = [&](int r, float o[4]) {
+    if constexpr (kZcShared) {
+      Quad<float>::ld(zq + r * Z, o);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) o[j] = rz[r][j];
+    }
+  };
   const float mdt = -a.dt;
   // Source box rows and z range of this item (the plane test is separate).
   const bool src_row = a.snc > 0 && yE >= a.sy0 && yE < a.sy0 + a.sny &&
@@ -352,12 +389,12 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
 #pragma unroll
       for (int c = 0; c < 3; ++c) Q::ld(Hs + c * RHZ + ieH, ho[c]);
       float pa[4], pb[4], ikh[4], bh[4], ch[4];
-      Quad<float>::ld(zq + 3 * Z, ikh);
+      zload(3, ikh);
       if (pml) {
         Q::ld(Ps + pH, pa);
         Q::ld(Ps + RH * Pp + pH, pb);
-        Quad<float>::ld(zq + 4 * Z, bh);
-        Quad<float>::ld(zq + 5 * Z, ch);
+        zload(4, bh);
+        zload(5, ch);
       }
       float hx[4], hy[4], hz[4];
 #pragma unroll
@@ -421,12 +458,12 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       }
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
       float pa[4], pb[4], ike[4], be[4], ce[4];
-      Quad<float>::ld(zq, ike);
+      zload(0, ike);
       if (pml) {
         Q::ld(Ps + 2 * RH * Pp + pE, pa);
         Q::ld(Ps + 3 * RH * Pp + pE, pb);
-        Quad<float>::ld(zq + Z, be);
-        Quad<float>::ld(zq + 2 * Z, ce);
+        zload(1, be);
+        zload(2, ce);
       }
       const bool src = src_row && x >= a.sx0 && x < a.sx0 + a.snx;
       float enew[3][4];
@@ -547,27 +584,6 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
     p2 = next(p2);
   }
 }
-
-// (zz, tile_y) shapes of the lean kernel: the streamed kernel's tile heights
-// for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
-#define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
-// Taller binary16 tiles (half the shared memory per row): 16 warps per CTA
-// hide more latency than 9 and the y halo is half as large per cell.
-#define PJZ_LEAN_SHAPES_F16(X_) X_(64, 28)
-
-// Block bound of a lean kernel instantiation: one CTA per SM (the ring and
-// staging buffers take most of the shared memory), 12 warps, or 16 for the
-// tall binary16 tiles (whose registers are capped at 128 by that).
-constexpr bool lean_tall_shape(int zc, int tyc) {
-#define PJZ_IS_TALL(ZC, TYC) (zc == ZC && tyc == TYC) ||
-  return PJZ_LEAN_SHAPES_F16(PJZ_IS_TALL) false;
-#undef PJZ_IS_TALL
-}
-template <int ZC, int TYC, typename T>
-struct LeanBounds {
-  static constexpr int threads = sizeof(T) == 2 && lean_tall_shape(ZC, TYC) ? 512 : 384;
-  static constexpr int blocks = 1;
-};
 
 template <int ZC, int TYC, typename T>
 __global__ void __launch_bounds__(LeanBounds<ZC, TYC, T>::threads,

@@ -61,8 +61,9 @@ struct RenderArgs {
   float* out;           // (3, xx, yy, zz)
   int ll, xx, yy, zz, m, simple;
   int group;            // layers staged together (1 .. ll)
-  uint32_t col_magic;   // render_col_magic(patch columns)
-  uint32_t row_magic;   // render_col_magic(patch rows)
+  uint64_t col_magic;   // render_col_magic(patch columns)
+  uint64_t row_magic;   // render_col_magic(patch rows)
+  uint64_t zq_magic;    // render_col_magic(zz / 4), when zz % 4 == 0
   float pos[kRenderMaxLayers - 1];  // interface positions, increasing
 };
 
@@ -95,10 +96,11 @@ PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
 
 // t / d for the patches' flat indices: floor(t * ceil(2^32 / d) / 2^32)
 // equals floor(t / d) while t * d < 2^32, which the host's limits keep.
-PJZ_HD uint32_t render_col_magic(uint32_t d) {
-  return (uint32_t)((((uint64_t)1 << 32) + d - 1) / d);
+// (The magic is 2^32 itself for d = 1, hence 64 bits.)
+PJZ_HD uint64_t render_col_magic(uint32_t d) {
+  return (((uint64_t)1 << 32) + d - 1) / d;
 }
-PJZ_HD int render_div(int t, uint32_t magic) {
+PJZ_HD int render_div(int t, uint64_t magic) {
   return (int)(((uint64_t)(uint32_t)t * magic) >> 32);
 }
 
@@ -181,17 +183,23 @@ PJZ_HD float render_u(const RenderArgs& a, int i) {
 // Statistics of one layer over the pixel window of component `c` at tile
 // row yl, from the staged patch `pf` (pixels) and `pinv` (their
 // reciprocals) with row stride `pc`; `u` holds render_u of 0 .. 2m-1.
-PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
-                                 const float* pf, const float* pinv, int pc,
-                                 const float* u) {
-  const int k = 2 * a.m;
-  const int ioff = c == 0 ? a.m : 0;           // rows shifted unless Ex
-  const int joff = k * yl + (c == 1 ? a.m : 0);  // columns shifted unless Ey
+// MC > 0: the magnification as a compile-time constant (same operations
+// in the same order, loops unrolled); MC = 0 takes a.m.
+template <int MC>
+PJZ_HD WindowStats render_window_m(const RenderArgs& a, int c, int yl,
+                                   const float* pf, const float* pinv, int pc,
+                                   const float* u) {
+  const int m = MC > 0 ? MC : a.m;
+  const int k = 2 * m;
+  const int ioff = c == 0 ? m : 0;           // rows shifted unless Ex
+  const int joff = k * yl + (c == 1 ? m : 0);  // columns shifted unless Ey
   float s = 0.f, si = 0.f, sxu = 0.f, syu = 0.f;
+#pragma unroll
   for (int i = 0; i < k; ++i) {
     const float ui = u[i];
     const float* rf = pf + (i + ioff) * pc + joff;
     const float* ri = pinv + (i + ioff) * pc + joff;
+#pragma unroll
     for (int j = 0; j < k; ++j) {
       const float f = rf[j];
       s += f;
@@ -207,6 +215,18 @@ PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
   w.gx = 12.0f * sxu / n;
   w.gy = 12.0f * syu / n;
   return w;
+}
+
+PJZ_HD WindowStats render_window(const RenderArgs& a, int c, int yl,
+                                 const float* pf, const float* pinv, int pc,
+                                 const float* u) {
+  switch (a.m) {
+    case 1: return render_window_m<1>(a, c, yl, pf, pinv, pc, u);
+    case 2: return render_window_m<2>(a, c, yl, pf, pinv, pc, u);
+    case 3: return render_window_m<3>(a, c, yl, pf, pinv, pc, u);
+    case 4: return render_window_m<4>(a, c, yl, pf, pinv, pc, u);
+    default: return render_window_m<0>(a, c, yl, pf, pinv, pc, u);
+  }
 }
 
 // The value from the fraction-weighted sums over the layers.
@@ -252,6 +272,19 @@ PJZ_HD int render_owner(const RenderArgs& a, const float* frac, int z) {
 
 PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) {
   return (((size_t)c * a.xx + x) * a.yy + y) * a.zz + z;
+}
+
+// Whether the outputs go out four z cells at a time (16-byte stores).
+PJZ_HD bool render_quads(const RenderArgs& a, const float* out) {
+  return a.zz % 4 == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
+}
+
+PJZ_HD void render_store4(float* p, const float v[4]) {
+#ifdef __CUDA_ARCH__
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+#else
+  for (int j = 0; j < 4; ++j) p[j] = v[j];
+#endif
 }
 
 // The CTA's phases, each a strided loop of thread `tid` of `nthr` (a
@@ -360,15 +393,42 @@ PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l
   }
 }
 
-// Phase 6: outputs.  Warp `w` of `nw` per (component, y) row, lane `lane`
-// of 32 along z (coalesced stores), writes the cells one layer fills; then
-// the CTA's threads share the interface-cut cells of every row (the same
-// few z for every row).  A row whose statistics are not all finite takes
-// the full mix at every z in the first loop.
+// Phase 6: outputs of the cells one layer fills.  With zz % 4 == 0 and a
+// 16-byte aligned output each thread writes four consecutive z cells at a
+// time (interface-cut cells among them get a placeholder that phase 7
+// overwrites after a barrier), z fastest over the CTA's threads: coalesced
+// 16-byte stores.  Otherwise warp `w` takes whole (component, y) rows, lane
+// `lane` along z, skipping cut cells.  A row whose statistics are not all
+// finite takes the full mix at every z here.
 PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
                              int y0, int ny, int w, int nw, int lane,
                              float* out) {
   const int LZ = a.ll * a.zz;
+  const int tid = w * 32 + lane, nthr = nw * 32;
+  if (render_quads(a, out)) {
+    const int zq = a.zz >> 2;
+    for (int c = 0; c < 3; ++c)
+      for (int t = tid; t < ny * zq; t += nthr) {
+        const int yl = render_div(t, a.zq_magic), z = 4 * (t - yl * zq);
+        const int cy = c * kRenderTileY + yl;
+        float v[4];
+        if (s.yfin[cy]) {
+          const float* iv = s.ival + cy * a.ll;
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const int o = s.owner[c * a.zz + z + j];
+            v[j] = o >= 0 ? iv[o] : 0.f;
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            v[j] = render_value(a, c, s.st + cy * a.ll, s.frac + c * LZ,
+                                s.mid + c * LZ, z + j);
+        }
+        render_store4(out + render_out_index(a, c, x, y0 + yl, z), v);
+      }
+    return;
+  }
   for (int c = 0; c < 3; ++c)
     for (int yl = w; yl < ny; yl += nw) {
       const int cy = c * kRenderTileY + yl;
@@ -385,7 +445,14 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
           row[z] = render_value(a, c, st, s.frac + c * LZ, s.mid + c * LZ, z);
       }
     }
-  const int tid = w * 32 + lane, nthr = nw * 32;
+}
+
+// Phase 7 (after a barrier): the interface-cut cells of every row with
+// finite statistics, shared over the CTA's threads (the same few z for
+// every row).
+PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int x,
+                                   int y0, int ny, int tid, int nthr, float* out) {
+  const int LZ = a.ll * a.zz;
   for (int c = 0; c < 3; ++c)
     for (int t = tid; t < s.ncut[c] * kRenderTileY; t += nthr) {
       const int yl = t % kRenderTileY, z = s.cut[c * a.zz + t / kRenderTileY];
@@ -418,6 +485,8 @@ __global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a)
   }
   __syncthreads();
   render_phase_out(a, s, x, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);
+  __syncthreads();  // placeholders of cut cells are written before phase 7
+  render_phase_cut_cells(a, s, x, y0, ny, tid, nthr, a.out);
 }
 #endif
 

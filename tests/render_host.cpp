@@ -46,6 +46,7 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   a.group = group > 0 && group < ll ? group : ll;
   a.col_magic = render_col_magic((uint32_t)render_patch_cols(m));
   a.row_magic = render_col_magic((uint32_t)render_patch_rows(m));
+  a.zq_magic = zz % 4 == 0 ? render_col_magic((uint32_t)(zz / 4)) : 0;
   for (int i = 0; i + 1 < ll; ++i) a.pos[i] = pos[i];
   g_render_layer_floats = (size_t)(2 * m * xx) * (2 * m * yy);
   g_render_bad = 0;
@@ -67,6 +68,8 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
       }
       for (int t = 0; t < kThreads; ++t)
         render_phase_out(a, s, x, y0, ny, t >> 5, kThreads >> 5, t & 31, a.out);
+      for (int t = 0; t < kThreads; ++t)
+        render_phase_cut_cells(a, s, x, y0, ny, t, kThreads, a.out);
     }
   for (size_t i = 0; i < kGuard; ++i) {
     uint32_t lo, hi;
