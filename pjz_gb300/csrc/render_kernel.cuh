@@ -466,7 +466,7 @@ PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int
 #if defined(__CUDACC__) && defined(PJZ_RENDER_KERNEL)  // kern_render.cu only
 // grid (xx, ceil(yy / kRenderTileY)), a multiple of 32 threads (at least
 // 96); dynamic shared memory render_smem_floats(ll, zz, m, group) floats.
-__global__ void __launch_bounds__(256) render_epsilon_kernel(const RenderArgs a) {
+__global__ void __launch_bounds__(256, 6) render_epsilon_kernel(const RenderArgs a) {
   extern __shared__ __align__(16) float rsm[];
   const int x = blockIdx.x, y0 = blockIdx.y * kRenderTileY;
   const int ny = min(kRenderTileY, a.yy - y0);
