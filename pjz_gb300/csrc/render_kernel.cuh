@@ -351,24 +351,43 @@ inline void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
 
 // Phase 4, per group of layers l0 .. l0 + ng - 1: their pixel patches for
 // the CTA at (x, y0) with ny tile rows (the columns its windows cover:
-// 2m*ny + m), one flat index over (layer, row, column).
+// 2m*ny + m), one flat index over (layer, row, column).  Each thread
+// issues the loads of kRenderStageBatch of its pixels before it uses any,
+// so their memory latencies overlap instead of adding up.
+constexpr int kRenderStageBatch = 8;
+
 PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
                                int ng, int x, int y0, int ny, int tid, int nthr) {
   const int k = 2 * a.m, pc = render_patch_cols(a.m);
   const int cols = k * ny + a.m, rows = ng * render_patch_rows(a.m);
   const int PX = k * a.xx, PY = k * a.yy;
-  for (int t = tid; t < rows * pc; t += nthr) {
-    const int gr = render_div(t, a.col_magic);  // (layer, row) of the group
-    const int cc = t - gr * pc;
-    if (cc >= cols) continue;
-    const int g = render_div(gr, a.row_magic);  // layer of the group
-    const int r = gr - g * render_patch_rows(a.m);
-    const int px = render_imax(k * x - a.m + r, 0);
-    const int py = render_imax(k * y0 - a.m + cc, 0);
-    const float* L = a.layers + (size_t)(l0 + g) * PX * PY;
-    const float f = render_load(L, (size_t)px * PY + py);
-    s.pf[t] = f;
-    s.pinv[t] = 1.0f / f;
+  const int n = rows * pc;
+  for (int t0 = tid; t0 < n; t0 += kRenderStageBatch * nthr) {
+    float f[kRenderStageBatch];
+#pragma unroll
+    for (int b = 0; b < kRenderStageBatch; ++b) {
+      const int t = t0 + b * nthr;
+      const int gr = render_div(t, a.col_magic);  // (layer, row) of the group
+      const int cc = t - gr * pc;
+      f[b] = 0.f;
+      if (t < n && cc < cols) {
+        const int g = render_div(gr, a.row_magic);  // layer of the group
+        const int r = gr - g * render_patch_rows(a.m);
+        const int px = render_imax(k * x - a.m + r, 0);
+        const int py = render_imax(k * y0 - a.m + cc, 0);
+        const float* L = a.layers + (size_t)(l0 + g) * PX * PY;
+        f[b] = render_load(L, (size_t)px * PY + py);
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < kRenderStageBatch; ++b) {
+      const int t = t0 + b * nthr;
+      const int gr = render_div(t, a.col_magic);
+      if (t < n && t - gr * pc < cols) {
+        s.pf[t] = f[b];
+        s.pinv[t] = 1.0f / f[b];
+      }
+    }
   }
 }
 
