@@ -1393,7 +1393,11 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
   const bool zq_exact =
       (uint64_t)kRenderTileY * (zz / 4) * (uint64_t)(zz / 4) < ((uint64_t)1 << 32);
-  if (smem > kSmemMax || !exact(group) || !zq_exact || yblocks > 65535)
+  const bool layer_fits =  // pixel offsets within a layer are 32-bit
+      (uint64_t)(2 * magnification) * xx * (uint64_t)(2 * magnification) * yy <
+      ((uint64_t)1 << 31);
+  if (smem > kSmemMax || !exact(group) || !zq_exact || !layer_fits ||
+      yblocks > 65535)
     return fail(PJZFDTD_ERR_INVALID,
                 "zz = %d with %d layers at magnification %d (or yy = %d) "
                 "exceeds one CTA's reach", zz, ll, magnification, yy);
@@ -1409,7 +1413,7 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   a.group = group;
   a.col_magic = render_col_magic((uint32_t)pcol);
   a.row_magic = render_col_magic((uint32_t)prow);
-  a.zq_magic = zz % 4 == 0 ? render_col_magic((uint32_t)(zz / 4)) : 0;
+  a.zq_magic = zz % 4 == 0 && zz >= 8 ? render_col_magic((uint32_t)(zz / 4)) : 0;
   for (int i = 0; i + 1 < ll; ++i) a.pos[i] = interface_positions[i];
   const RenderKernel k = render_kernel_ptr();
   if (smem > 48 * 1024)

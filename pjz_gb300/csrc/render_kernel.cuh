@@ -61,9 +61,9 @@ struct RenderArgs {
   float* out;           // (3, xx, yy, zz)
   int ll, xx, yy, zz, m, simple;
   int group;            // layers staged together (1 .. ll)
-  uint64_t col_magic;   // render_col_magic(patch columns)
-  uint64_t row_magic;   // render_col_magic(patch rows)
-  uint64_t zq_magic;    // render_col_magic(zz / 4), when zz % 4 == 0
+  uint32_t col_magic;   // render_col_magic(patch columns)
+  uint32_t row_magic;   // render_col_magic(patch rows)
+  uint32_t zq_magic;    // render_col_magic(zz / 4), when render_quads
   float pos[kRenderMaxLayers - 1];  // interface positions, increasing
 };
 
@@ -96,12 +96,16 @@ PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
 
 // t / d for the patches' flat indices: floor(t * ceil(2^32 / d) / 2^32)
 // equals floor(t / d) while t * d < 2^32, which the host's limits keep.
-// (The magic is 2^32 itself for d = 1, hence 64 bits.)
-PJZ_HD uint64_t render_col_magic(uint32_t d) {
-  return (((uint64_t)1 << 32) + d - 1) / d;
+// d >= 2, so the magic fits 32 bits.
+PJZ_HD uint32_t render_col_magic(uint32_t d) {
+  return (uint32_t)((((uint64_t)1 << 32) + d - 1) / d);
 }
-PJZ_HD int render_div(int t, uint64_t magic) {
+PJZ_HD int render_div(int t, uint32_t magic) {
+#ifdef __CUDA_ARCH__
+  return (int)__umulhi((uint32_t)t, magic);
+#else
   return (int)(((uint64_t)(uint32_t)t * magic) >> 32);
+#endif
 }
 
 // Shared-memory floats of one CTA staging `group` layers at once: occupancy
@@ -274,9 +278,23 @@ PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) 
   return (((size_t)c * a.xx + x) * a.yy + y) * a.zz + z;
 }
 
-// Whether the outputs go out four z cells at a time (16-byte stores).
+// Whether the outputs go out four z cells at a time (16-byte stores): zz a
+// multiple of 4 (at least 8) and a 16-byte aligned output.
 PJZ_HD bool render_quads(const RenderArgs& a, const float* out) {
-  return a.zz % 4 == 0 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
+  return a.zz % 4 == 0 && a.zz >= 8 && reinterpret_cast<uintptr_t>(out) % 16 == 0;
+}
+
+// Four consecutive owners (16-byte aligned: zz % 4 == 0 and z % 4 == 0).
+PJZ_HD void render_owner4(const int* p, int o[4]) {
+#ifdef __CUDA_ARCH__
+  const int4 v = *reinterpret_cast<const int4*>(p);
+  o[0] = v.x;
+  o[1] = v.y;
+  o[2] = v.z;
+  o[3] = v.w;
+#else
+  for (int j = 0; j < 4; ++j) o[j] = p[j];
+#endif
 }
 
 PJZ_HD void render_store4(float* p, const float v[4]) {
@@ -362,8 +380,10 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
   const int cols = k * ny + a.m, rows = ng * render_patch_rows(a.m);
   const int PX = k * a.xx, PY = k * a.yy;
   const int n = rows * pc;
+  const float* L0 = a.layers + (size_t)l0 * PX * PY;
   for (int t0 = tid; t0 < n; t0 += kRenderStageBatch * nthr) {
     float f[kRenderStageBatch];
+    unsigned live = 0;  // bit b: pixel t0 + b * nthr is staged
 #pragma unroll
     for (int b = 0; b < kRenderStageBatch; ++b) {
       const int t = t0 + b * nthr;
@@ -375,15 +395,15 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
         const int r = gr - g * render_patch_rows(a.m);
         const int px = render_imax(k * x - a.m + r, 0);
         const int py = render_imax(k * y0 - a.m + cc, 0);
-        const float* L = a.layers + (size_t)(l0 + g) * PX * PY;
-        f[b] = render_load(L, (size_t)px * PY + py);
+        // One layer holds fewer than 2^31 pixels (checked by the host).
+        f[b] = render_load(L0 + (size_t)g * PX * PY, (size_t)(px * PY + py));
+        live |= 1u << b;
       }
     }
 #pragma unroll
     for (int b = 0; b < kRenderStageBatch; ++b) {
       const int t = t0 + b * nthr;
-      const int gr = render_div(t, a.col_magic);
-      if (t < n && t - gr * pc < cols) {
+      if (live >> b & 1u) {
         s.pf[t] = f[b];
         s.pinv[t] = 1.0f / f[b];
       }
@@ -433,11 +453,10 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
         float v[4];
         if (s.yfin[cy]) {
           const float* iv = s.ival + cy * a.ll;
+          int o[4];
+          render_owner4(s.owner + c * a.zz + z, o);
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            const int o = s.owner[c * a.zz + z + j];
-            v[j] = o >= 0 ? iv[o] : 0.f;
-          }
+          for (int j = 0; j < 4; ++j) v[j] = o[j] >= 0 ? iv[o[j]] : 0.f;
         } else {
 #pragma unroll
           for (int j = 0; j < 4; ++j)

@@ -46,7 +46,7 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   a.group = group > 0 && group < ll ? group : ll;
   a.col_magic = render_col_magic((uint32_t)render_patch_cols(m));
   a.row_magic = render_col_magic((uint32_t)render_patch_rows(m));
-  a.zq_magic = zz % 4 == 0 ? render_col_magic((uint32_t)(zz / 4)) : 0;
+  a.zq_magic = zz % 4 == 0 && zz >= 8 ? render_col_magic((uint32_t)(zz / 4)) : 0;
   for (int i = 0; i + 1 < ll; ++i) a.pos[i] = pos[i];
   g_render_layer_floats = (size_t)(2 * m * xx) * (2 * m * yy);
   g_render_bad = 0;
