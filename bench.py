@@ -445,15 +445,20 @@ def f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells):
   per_launch = int(np.prod(wl.domain))
   achieved = BYTES_PER_CELL_F16 * per_launch / (launch_ms / 1e3) / 1e9
   peak, peak_kind = _peaks()
+  cfg = plan.launch_config()
+  bpc = None
+  if cfg["kernel"] == 3 and cfg["steps_per_pass"] == 1 and cfg["tile_y"] == 14:
+    bpc, _ = _profile_traffic(f"yee_lean_f16_{args.workload}")
   return {"value": world * cells / (ms / 1e3) / 1e9, "unit": UNIT,
           "ms_per_step": ms, "dtype": "binary16 storage, f32 arithmetic",
-          "launch": plan.launch_config(),
+          "launch": cfg,
           "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": f"hbm_gbs of {peak_kind}",
                        "kernel": "yee_lean_kernel (binary16)",
                        "algorithmic_bytes_per_launch": BYTES_PER_CELL_F16 * per_launch,
-                       "launch_ms": launch_ms},
+                       "launch_ms": launch_ms,
+                       "traffic": None if bpc is None else bpc * per_launch},
           "accuracy": "rel-L2 vs the FP64 oracle: asserted and printed by "
                       "tests/test_gpu_f16.py (c0) and "
                       "tests/test_gpu_full_length.py (c1)"}
