@@ -1411,6 +1411,11 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   a.m = magnification;
   a.simple = use_simple_averaging != 0;
   a.group = group;
+  a.sorted = 1;  // nondecreasing without NaN: owners by comparison
+  for (int i = 0; i + 1 < ll; ++i)
+    if (interface_positions[i] != interface_positions[i] ||
+        (i > 0 && !(interface_positions[i - 1] <= interface_positions[i])))
+      a.sorted = 0;
   a.col_magic = render_col_magic((uint32_t)pcol);
   a.row_magic = render_col_magic((uint32_t)prow);
   a.zq_magic = zz % 4 == 0 && zz >= 8 ? render_col_magic((uint32_t)(zz / 4)) : 0;

@@ -19,16 +19,17 @@
 // (subpixel smoothing, diagonal of the interface projection only).
 //
 // One CTA per (x, block of kRenderTileY y cells), all three components.
-// It tabulates the z occupancy of each component's cells, then, a group of
+// It tabulates the layer that fills each component's z cells, then, a group of
 // layers at a time (as many as the host fits in shared memory), stages the
 // layers' pixel patches that the block's windows cover (3m rows x
 // (2m*ny + m) columns each, edge pixels repeated) with each pixel's
 // reciprocal computed once, computes every window's statistics from the
 // patches, and finally writes the (component, y, z) outputs with z fastest,
-// coalesced.  A z cell that lies wholly inside one
-// layer (its fraction exactly 1, all others exactly 0) has the same value at
-// every such z of a column: it is computed once per (y, layer) and copied,
-// and only the cells an interface cuts take the full mix.  Both give the
+// coalesced.  With interface positions in nondecreasing order, a z cell
+// that lies wholly inside one layer (its fraction exactly 1, all others
+// exactly 0) has the same value at every such z of a column: it is
+// computed once per (y, layer) and copied, and only the cells an interface
+// cuts take the full mix (out-of-order or NaN positions: every cell).  Both give the
 // same floats when every layer's window statistics at that (x, y) are
 // finite (the full mix then adds exact zeros to that layer's terms); where
 // one is not (a zero pixel makes the mean of the inverse infinite, a NaN
@@ -61,6 +62,7 @@ struct RenderArgs {
   float* out;           // (3, xx, yy, zz)
   int ll, xx, yy, zz, m, simple;
   int group;            // layers staged together (1 .. ll)
+  int sorted;           // positions nondecreasing and free of NaN
   uint32_t col_magic;   // render_col_magic(patch columns)
   uint32_t row_magic;   // render_col_magic(patch rows)
   uint32_t zq_magic;    // render_col_magic(zz / 4), when render_quads
@@ -108,9 +110,9 @@ PJZ_HD int render_div(int t, uint32_t magic) {
 #endif
 }
 
-// Shared-memory floats of one CTA staging `group` layers at once: occupancy
-// frac / mid [3][ll][zz], the layer that fills each z cell [3][zz] (int, -1
-// when an interface cuts it), window statistics [3][kRenderTileY][ll] of 4
+// Shared-memory floats of one CTA staging `group` layers at once: the layer
+// that fills each z cell [3][zz] (int, -1 when an interface cuts it),
+// window statistics [3][kRenderTileY][ll] of 4
 // floats, one-layer values [3][kRenderTileY][ll], per (component, y)
 // whether every layer's statistics are finite [3][kRenderTileY] (int), the
 // pixel patches and their reciprocals [2][group][3m][2m*kRenderTileY + m],
@@ -118,7 +120,7 @@ PJZ_HD int render_div(int t, uint32_t magic) {
 // per component the z cells an interface cuts [3][zz] (int) and their
 // count [4] (int).
 PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group) {
-  return 6 * (size_t)ll * zz + 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
+  return 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
          3 * kRenderTileY +
          2 * (size_t)group * render_patch_rows(m) * render_patch_cols(m) + 2 * m +
          kRenderMaxLayers + 3 * (size_t)zz + 4;
@@ -126,8 +128,6 @@ PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group) {
 
 // The regions of one CTA's shared memory (render_smem_floats floats).
 struct RenderSmem {
-  float* frac;      // [3][ll][zz]
-  float* mid;       // [3][ll][zz]
   int* owner;       // [3][zz]
   WindowStats* st;  // [3][kRenderTileY][ll]
   float* ival;      // [3][kRenderTileY][ll]
@@ -142,12 +142,10 @@ struct RenderSmem {
 };
 
 PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m, int group) {
-  const int LZ = ll * zz, TL = kRenderTileY * ll;
+  const int TL = kRenderTileY * ll;
   const int np = group * render_patch_rows(m) * render_patch_cols(m);
   RenderSmem s;
-  s.frac = sm;
-  s.mid = s.frac + 3 * LZ;
-  s.owner = reinterpret_cast<int*>(s.mid + 3 * LZ);
+  s.owner = reinterpret_cast<int*>(sm);
   s.st = reinterpret_cast<WindowStats*>(s.owner + 3 * zz);
   s.ival = reinterpret_cast<float*>(s.st + 3 * TL);
   s.yfin = reinterpret_cast<int*>(s.ival + 3 * TL);
@@ -168,12 +166,17 @@ PJZ_HD bool render_finite(const WindowStats& w) {
 // Filled fraction of z cell `z` of component `c` by layer `l`, and the
 // offset of the filled part's midpoint from the cell centre.
 // `pos` holds the interface positions.
+// Clamp to [lo, hi] that keeps NaN (as pjz's jnp.clip does).
+PJZ_HD float render_clip(float v, float lo, float hi) {
+  return v != v ? v : fminf(fmaxf(v, lo), hi);
+}
+
 PJZ_HD void render_occupancy(const RenderArgs& a, const float* pos, int c, int l,
                              int z, float* frac, float* mid) {
   const float lo = c == 2 ? (float)z : (float)z - 0.5f;
   const float hi = c == 2 ? (float)z + 1.0f : (float)z + 0.5f;
-  const float b = l == 0 ? lo : fminf(fmaxf(pos[l - 1], lo), hi);
-  const float t = l == a.ll - 1 ? hi : fminf(fmaxf(pos[l], lo), hi);
+  const float b = l == 0 ? lo : render_clip(pos[l - 1], lo, hi);
+  const float t = l == a.ll - 1 ? hi : render_clip(pos[l], lo, hi);
   *frac = (t - b) / (hi - lo);
   *mid = 0.5f * (b + t) - 0.5f * (lo + hi);
 }
@@ -245,17 +248,19 @@ PJZ_HD float render_mix(const RenderArgs& a, int c, float avg, float inv,
 }
 
 // Value of component `c` at z from the window statistics of its (x, y)
-// (st[l]) and the occupancy of its z cells (frac / mid [l * zz + z]).
-PJZ_HD float render_value(const RenderArgs& a, int c, const WindowStats* st,
-                          const float* frac, const float* mid, int z) {
+// (st[l]) and the occupancy of its z cell by each layer (interface
+// positions `pos`).
+PJZ_HD float render_value(const RenderArgs& a, const float* pos, int c,
+                          const WindowStats* st, int z) {
   float avg = 0.f, inv = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
   for (int l = 0; l < a.ll; ++l) {
-    const float f = frac[l * a.zz + z];
+    float f, mid;
+    render_occupancy(a, pos, c, l, z, &f, &mid);
     avg += st[l].mean * f;
     inv += st[l].inv * f;
     gx += st[l].gx * f;
     gy += st[l].gy * f;
-    gz += st[l].mean * f * mid[l * a.zz + z];
+    gz += st[l].mean * f * mid;
   }
   return render_mix(a, c, avg, inv, gx, gy, gz);
 }
@@ -267,11 +272,32 @@ PJZ_HD float render_interior(const RenderArgs& a, int c, const WindowStats& w) {
   return render_mix(a, c, 0.f + w.mean, 0.f + w.inv, 0.f + w.gx, 0.f + w.gy, 0.f);
 }
 
-// The layer whose fraction of z cell `z` is exactly 1, else -1.
-PJZ_HD int render_owner(const RenderArgs& a, const float* frac, int z) {
-  for (int l = 0; l < a.ll; ++l)
-    if (frac[l * a.zz + z] == 1.0f) return l;
+// The layer whose fraction of z cell `z` of component `c` is exactly 1,
+// else -1 (the definition render_owner_sorted is tested against).
+PJZ_HD int render_owner(const RenderArgs& a, const float* pos, int c, int z) {
+  for (int l = 0; l < a.ll; ++l) {
+    float f, mid;
+    render_occupancy(a, pos, c, l, z, &f, &mid);
+    if (f == 1.0f) return l;
+  }
   return -1;
+}
+
+// render_owner for nondecreasing positions without NaN, by comparisons:
+// with no interface strictly inside the cell (lo, hi) the layer above the
+// k interfaces at or below lo spans it (fraction (hi - lo) / (hi - lo) = 1,
+// every other layer 0); with one inside, every layer stops short of lo or
+// hi and the fractions are exact differences below 1.
+PJZ_HD int render_owner_sorted(const RenderArgs& a, const float* pos, int c, int z) {
+  const float lo = c == 2 ? (float)z : (float)z - 0.5f;
+  const float hi = c == 2 ? (float)z + 1.0f : (float)z + 0.5f;
+  int k = 0;
+  bool cut = false;
+  for (int i = 0; i + 1 < a.ll; ++i) {
+    k += pos[i] <= lo;
+    cut |= pos[i] > lo && pos[i] < hi;
+  }
+  return cut ? -1 : k;
 }
 
 PJZ_HD size_t render_out_index(const RenderArgs& a, int c, int x, int y, int z) {
@@ -321,18 +347,16 @@ PJZ_HD void render_phase_setup(const RenderArgs& a, const RenderSmem& s, int tid
   for (int t = tid; t < 3 * kRenderTileY; t += nthr) s.yfin[t] = 1;
 }
 
-// Phase 2 (after the positions are in shared memory): z occupancy and the
-// filling layer of every component's z cells.
+// Phase 2 (after the positions are in shared memory): the filling layer of
+// every component's z cells.  Out-of-order (or NaN) positions make some
+// layers' fractions negative or NaN, so no cell has a single owner there:
+// every cell takes the full mix.
 PJZ_HD void render_phase_occupancy(const RenderArgs& a, const RenderSmem& s,
                                    int tid, int nthr) {
-  const int LZ = a.ll * a.zz;
-  for (int c = 0; c < 3; ++c)
-    for (int z = tid; z < a.zz; z += nthr) {
-      for (int l = 0; l < a.ll; ++l)
-        render_occupancy(a, s.pos, c, l, z, &s.frac[c * LZ + l * a.zz + z],
-                         &s.mid[c * LZ + l * a.zz + z]);
-      s.owner[c * a.zz + z] = render_owner(a, s.frac + c * LZ, z);
-    }
+  for (int t = tid; t < 3 * a.zz; t += nthr) {
+    const int c = t >= 2 * a.zz ? 2 : (t >= a.zz ? 1 : 0), z = t - c * a.zz;
+    s.owner[t] = a.sorted ? render_owner_sorted(a, s.pos, c, z) : -1;
+  }
 }
 
 // Phase 3 (beside the first group's staging, after a barrier that follows
@@ -442,7 +466,6 @@ PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l
 PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
                              int y0, int ny, int w, int nw, int lane,
                              float* out) {
-  const int LZ = a.ll * a.zz;
   const int tid = w * 32 + lane, nthr = nw * 32;
   if (render_quads(a, out)) {
     const int zq = a.zz >> 2;
@@ -460,8 +483,7 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
         } else {
 #pragma unroll
           for (int j = 0; j < 4; ++j)
-            v[j] = render_value(a, c, s.st + cy * a.ll, s.frac + c * LZ,
-                                s.mid + c * LZ, z + j);
+            v[j] = render_value(a, s.pos, c, s.st + cy * a.ll, z + j);
         }
         render_store4(out + render_out_index(a, c, x, y0 + yl, z), v);
       }
@@ -480,7 +502,7 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
         }
       } else {
         for (int z = lane; z < a.zz; z += 32)
-          row[z] = render_value(a, c, st, s.frac + c * LZ, s.mid + c * LZ, z);
+          row[z] = render_value(a, s.pos, c, st, z);
       }
     }
 }
@@ -490,14 +512,13 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
 // every row).
 PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int x,
                                    int y0, int ny, int tid, int nthr, float* out) {
-  const int LZ = a.ll * a.zz;
   for (int c = 0; c < 3; ++c)
     for (int t = tid; t < s.ncut[c] * kRenderTileY; t += nthr) {
       const int yl = t % kRenderTileY, z = s.cut[c * a.zz + t / kRenderTileY];
       const int cy = c * kRenderTileY + yl;
       if (yl < ny && s.yfin[cy])
-        out[render_out_index(a, c, x, y0 + yl, z)] = render_value(
-            a, c, s.st + cy * a.ll, s.frac + c * LZ, s.mid + c * LZ, z);
+        out[render_out_index(a, c, x, y0 + yl, z)] =
+            render_value(a, s.pos, c, s.st + cy * a.ll, z);
     }
 }
 

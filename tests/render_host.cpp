@@ -44,6 +44,9 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   a.m = m;
   a.simple = simple != 0;
   a.group = group > 0 && group < ll ? group : ll;
+  a.sorted = 1;
+  for (int i = 0; i + 1 < ll; ++i)
+    if (pos[i] != pos[i] || (i > 0 && !(pos[i - 1] <= pos[i]))) a.sorted = 0;
   a.col_magic = render_col_magic((uint32_t)render_patch_cols(m));
   a.row_magic = render_col_magic((uint32_t)render_patch_rows(m));
   a.zq_magic = zz % 4 == 0 && zz >= 8 ? render_col_magic((uint32_t)(zz / 4)) : 0;
@@ -79,4 +82,17 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
   }
   memcpy(out, a.out, out_floats * sizeof(float));
   return g_render_bad;
+}
+
+// Number of (component, z) cells, z in [zlo, zhi), whose owner by
+// comparison differs from the owner by exact fractions, for `ll` layers
+// with interface positions `pos` (nondecreasing, no NaN).
+extern "C" int render_owner_mismatches(const float* pos, int ll, int zlo, int zhi) {
+  RenderArgs a = {};
+  a.ll = ll;
+  int bad = 0;
+  for (int c = 0; c < 3; ++c)
+    for (int z = zlo; z < zhi; ++z)
+      bad += render_owner(a, pos, c, z) != render_owner_sorted(a, pos, c, z);
+  return bad;
 }

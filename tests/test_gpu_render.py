@@ -112,3 +112,21 @@ def test_gpu_nonfinite_window_matches_oracle_pattern(native, bad, simple):
   np.testing.assert_array_equal(np.isinf(got), np.isinf(want))
   ok = np.isfinite(want)
   np.testing.assert_allclose(got[ok], want[ok], rtol=2e-5, atol=0)
+
+
+@pytest.mark.parametrize("pos", [[6.5, 2.25, 8.0], [3.0, float("nan"), 5.5]])
+def test_gpu_unordered_or_nan_positions_take_the_full_mix(native, host, pos):
+  """Out-of-order or NaN interface positions: no cell has a single owner,
+  every cell takes the full mix -- bit-equal to the host emulation and
+  following the oracle (NaN where it is NaN)."""
+  rng = np.random.default_rng(12)
+  m, zz = 2, 12
+  layers = rng.uniform(1.0, 12.0, (4, 2 * m * 5, 2 * m * 37)).astype(np.float32)
+  pos = np.array(pos, np.float32)
+  got = _gpu(layers, pos, m, zz)
+  np.testing.assert_array_equal(got, render(host, layers, pos, m, zz, finite=False))
+  with np.errstate(divide="ignore", invalid="ignore"):
+    want = eo.epsilon(layers.astype(np.float64), pos.astype(np.float64), m, zz, False)
+  ok = np.isfinite(want)
+  np.testing.assert_array_equal(np.isfinite(got), ok)
+  np.testing.assert_allclose(got[ok], want[ok], rtol=2e-5, atol=1e-6)

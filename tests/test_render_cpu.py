@@ -34,6 +34,8 @@ def host(tmp_path_factory):
   I = ctypes.c_int
   h.render_host.argtypes = [P, I, I, I, I, I, P, I, I, P]
   h.render_host.restype = I
+  h.render_owner_mismatches.argtypes = [P, I, I, I]
+  h.render_owner_mismatches.restype = I
   return h
 
 
@@ -72,6 +74,24 @@ def test_matches_fp64_oracle(host, ll, xx, yy, zz, m, simple):
   np.testing.assert_allclose(got, want, rtol=2e-5, atol=0)
 
 
+def test_owner_by_comparison_matches_exact_fractions(host):
+  """For sorted positions without NaN the kernel finds each z cell's
+  filling layer by comparing positions with the cell bounds; it must name
+  the same layer as the exact-fraction test (fraction == 1) for interfaces
+  on cell edges and centres, ties (zero-thickness layers), infinities,
+  huge values, and random positions."""
+  rng = np.random.default_rng(5)
+  cases = [[0.5, 1.0], [2.0, 2.0, 2.0], [-np.inf, 3.5, np.inf], [1e30, 2e30],
+           [-1e30, 0.0], [4.5, 4.5, 5.0, 5.5], [0.25, 7.75]]
+  for ll in range(2, 17):
+    cases.append(np.sort(rng.uniform(-2, 12, ll - 1)))
+    cases.append(np.sort(rng.integers(-2, 24, ll - 1) / 2.0))
+    cases.append(np.sort(rng.integers(-8, 48, ll - 1) / 4.0))
+  for pos in cases:
+    pos = np.ascontiguousarray(pos, np.float32)
+    assert host.render_owner_mismatches(pos.ctypes.data, len(pos) + 1, -3, 16) == 0, pos
+
+
 @pytest.mark.parametrize("ll,m", [(5, 2), (16, 1), (3, 3)])
 def test_layer_groups_give_the_same_floats(host, ll, m):
   """Staging the layers in groups of any size (the library stages as many
@@ -83,6 +103,26 @@ def test_layer_groups_give_the_same_floats(host, ll, m):
   want = render(host, layers, pos, m, zz)
   for g in range(1, ll):
     np.testing.assert_array_equal(render(host, layers, pos, m, zz, group=g), want)
+
+
+def test_unsorted_positions_follow_the_oracle(host):
+  """Positions out of order take the exact-fraction owner test; the result
+  still follows the oracle (which applies pjz's formulas as they are)."""
+  rng = np.random.default_rng(11)
+  m, zz = 1, 10
+  layers = rng.uniform(1.0, 12.0, (4, 2 * m * 3, 2 * m * 5))
+  for pos in ([6.5, 2.25, 8.0], [3.0, np.nan, 5.5]):
+    _unsorted_case(host, layers, np.array(pos, np.float32), m, zz)
+
+
+def _unsorted_case(host, layers, pos, m, zz):
+  got = render(host, layers, pos, m, zz, finite=False)
+  with np.errstate(divide="ignore", invalid="ignore"):
+    want = eo.epsilon(layers.astype(np.float32).astype(np.float64),
+                      pos.astype(np.float64), m, zz, False)
+  ok = np.isfinite(want)
+  np.testing.assert_array_equal(np.isfinite(got), ok)
+  np.testing.assert_allclose(got[ok], want[ok], rtol=2e-5, atol=1e-6)
 
 
 def test_reference_layer_tables(host):
