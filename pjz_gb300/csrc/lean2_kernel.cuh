@@ -62,10 +62,9 @@ struct Lean2Geom {
 };
 
 // Warps of the lean two-step kernel: one item per (buffer row, quad) over
-// the NR = tile_y + 3 rows of level 1, interior warps then PML warps.
-__host__ __device__ inline int lean2_warps(int Z, int ty, int plo, int phi) {
-  return ((ty + 3) * lean_quads_interior(Z, plo, phi) + 31) / 32 +
-         ((ty + 3) * lean_quads_pml(plo, phi) + 31) / 32;
+// the NR = tile_y + 3 rows of level 1 (lean_item).
+__host__ __device__ inline int lean2_warps(int Z, int ty, int plo, int phi, int esz) {
+  return lean_warps(Z, ty + 3, plo, phi, esz);
 }
 
 template <int ZC, int TYC, typename T>
@@ -234,18 +233,11 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
   }
 
   // ---------------- compute warps ----------------
-  const int QI = (Z - a.plo - a.phi) >> 2;
-  const int QP = (a.plo + a.phi) >> 2;
-  const int nwi = (NR * QI + 31) >> 5;
-  const bool pml = (tid >> 5) >= nwi;  // warp-uniform
-  const int it = pml ? tid - (nwi << 5) : tid;
-  const int Qn = pml ? QP : QI;
-  const int ra = Qn > 0 ? it / Qn : NR;  // buffer row (y = y0 - 2 + ra)
-  const int qi = it - ra * Qn;
-  const int lq = a.plo >> 2;
-  const int q = pml ? (qi < lq ? qi : (Z >> 2) - QP + qi) : lq + qi;
-  const int z0 = 4 * q;
-  const int col = 4 * qi;
+  const LeanItem item = lean_item(tid, Z, NR, a.plo, a.phi, (int)ES);
+  const bool pml = item.pml;
+  const int ra = item.row;  // buffer row (y = y0 - 2 + ra)
+  const int z0 = item.z0;
+  const int col = item.col;
   const int y = y0 - 2 + ra;
   const bool in_y = ra < NR && y >= 0 && y < Y;
   const bool do_h1 = in_y;                          // rows 0 .. NR-1

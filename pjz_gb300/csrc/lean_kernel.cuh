@@ -32,19 +32,71 @@
 
 namespace pjzfdtd {
 
-// Quads per row outside / inside the z-PML slabs and the warps that hold
-// one item each for the tile_y + 1 rows of the H phase.
+// Quads per row outside / inside the z-PML slabs.
 __host__ __device__ inline int lean_quads_interior(int Z, int plo, int phi) {
   return (Z - plo - phi) / 4;
 }
 __host__ __device__ inline int lean_quads_pml(int plo, int phi) {
   return (plo + phi) / 4;
 }
-__host__ __device__ inline int lean_warps_interior(int Z, int ty, int plo, int phi) {
-  return ((ty + 1) * lean_quads_interior(Z, plo, phi) + 31) / 32;
+
+// Items of the lean kernels: one (buffer row, z-quad) per compute thread
+// over `rows` buffer rows.
+//
+// Split mapping (FP32 storage, zz 64, plo + phi <= 32): a 128-bit shared
+// access of a warp is served 8 lanes at a time, and quad q of any row sits
+// in bank group q % 8 (rows are 256 bytes).  Each row's 16 quads split into
+// an edge set -- quads [0, 8 - ph) and [16 - ph, 16), ph = phi / 4, which
+// holds every z-PML quad -- and an interior set [8 - ph, 16 - ph); each
+// set has one quad per bank group.  Edge warps take the edge sets of four
+// rows (8 lanes per row), interior warps the interior sets, so every quad
+// access is free of bank conflicts; edge warps branch per lane on the
+// z-PML update.
+//
+// Otherwise: interior warps first (the quads between the slabs, row-major),
+// then z-PML warps (the slab quads), so the z-PML branch is warp-uniform.
+struct LeanItem {
+  int row;   // buffer row (rows and beyond: idle)
+  int z0;    // first z of the quad
+  int col;   // z-PML state column of z0 (z-PML quads)
+  bool pml;  // a z-PML quad
+};
+
+__host__ __device__ inline bool lean_split(int Z, int plo, int phi, int esz) {
+  return esz == 4 && Z == 64 && plo + phi <= 32;
 }
-__host__ __device__ inline int lean_warps_pml(int ty, int plo, int phi) {
-  return ((ty + 1) * lean_quads_pml(plo, phi) + 31) / 32;
+
+__host__ __device__ inline int lean_warps(int Z, int rows, int plo, int phi, int esz) {
+  if (lean_split(Z, plo, phi, esz)) return 2 * ((rows + 3) / 4);
+  return (rows * lean_quads_interior(Z, plo, phi) + 31) / 32 +
+         (rows * lean_quads_pml(plo, phi) + 31) / 32;
+}
+
+__host__ __device__ inline LeanItem lean_item(int tid, int Z, int rows, int plo,
+                                              int phi, int esz) {
+  const int lq = plo / 4, pq = phi / 4, nq = Z / 4;
+  LeanItem it;
+  int q;
+  if (lean_split(Z, plo, phi, esz)) {
+    const int ne = (rows + 3) / 4;  // edge warps
+    const int w = tid >> 5, j = tid & 7;
+    const bool edge = w < ne;
+    it.row = 4 * (edge ? w : w - ne) + ((tid >> 3) & 3);
+    q = edge ? (j < 8 - pq ? j : j + 8) : 8 - pq + j;
+  } else {
+    const int QI = lean_quads_interior(Z, plo, phi), QP = lean_quads_pml(plo, phi);
+    const int nwi = (rows * QI + 31) / 32;
+    const bool pw = (tid >> 5) >= nwi;
+    const int i = pw ? tid - 32 * nwi : tid;
+    const int Qn = pw ? QP : QI;
+    it.row = Qn > 0 ? i / Qn : rows;
+    const int qi = i - it.row * Qn;
+    q = pw ? (qi < lq ? qi : nq - QP + qi) : lq + qi;
+  }
+  it.pml = q < lq || q >= nq - pq;
+  it.z0 = 4 * q;
+  it.col = 4 * (q < lq ? q : lq + q - (nq - pq));
+  return it;
 }
 
 // Shared-memory geometry of one lean CTA for storage type T (bytes).  The
@@ -311,18 +363,11 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   // ---------------- compute warps ----------------
   // Item of this thread: interior warps first, then PML warps; item i is
   // (buffer row i / Qn, quad i % Qn of the warp kind's quads).
-  const int QI = (Z - a.plo - a.phi) >> 2;
-  const int QP = (a.plo + a.phi) >> 2;
-  const int nwi = (RH * QI + 31) >> 5;
-  const bool pml = (tid >> 5) >= nwi;  // warp-uniform
-  const int it = pml ? tid - (nwi << 5) : tid;
-  const int Qn = pml ? QP : QI;
-  const int rH = Qn > 0 ? it / Qn : RH;
-  const int qi = it - rH * Qn;
-  const int lq = a.plo >> 2;
-  const int q = pml ? (qi < lq ? qi : (Z >> 2) - QP + qi) : lq + qi;
-  const int z0 = 4 * q;
-  const int col = 4 * qi;  // z-PML state column of z0 (PML warps)
+  const LeanItem item = lean_item(tid, Z, RH, a.plo, a.phi, (int)ES);
+  const bool pml = item.pml;
+  const int rH = item.row;
+  const int z0 = item.z0;
+  const int col = item.col;  // z-PML state column of z0 (z-PML quads)
   const bool doH = rH < RH && y0 - 1 + rH >= 0 && y0 - 1 + rH < Y;
   const int yE = y0 + rH;
   const bool doE = rH < TY && yE < Y;

@@ -316,8 +316,7 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
                 "that are multiples of 4 (got %d, %d)",
                 Z, ty, p.pml_lo, p.pml_hi);
   }
-  const int warps = lean_warps_interior(Z, ty, p.pml_lo, p.pml_hi) +
-                    lean_warps_pml(ty, p.pml_lo, p.pml_hi);
+  const int warps = lean_warps(Z, ty + 1, p.pml_lo, p.pml_hi, pl->esz);
   const int bound = lean_kernel_threads(Z, ty, p.storage);
   if (warps * 32 + 32 > bound)
     return required ? fail(PJZFDTD_ERR_UNSUPPORTED, "lean tile needs %d warps",
@@ -355,7 +354,7 @@ int32_t resolve_lean2(pjzfdtd_plan* pl) {
     return fail(PJZFDTD_ERR_UNSUPPORTED,
                 "the lean two-step kernel needs (zz, tile_y) = (64, 14), got "
                 "(%d, %d)", Z, ty);
-  const int warps = lean2_warps(Z, ty, p.pml_lo, p.pml_hi);
+  const int warps = lean2_warps(Z, ty, p.pml_lo, p.pml_hi, pl->esz);
   if (warps * 32 + 32 > kLeanThreads)
     return fail(PJZFDTD_ERR_UNSUPPORTED, "lean two-step tile needs %d warps", warps);
   const int s2 = pl->stages2 & 0xff;

@@ -241,33 +241,42 @@ def pml_columns(Z, plo, phi):
   return z0s, pz
 
 
-def lean_items(Z, TY, plo, phi):
-  """Every compute thread's item in the lean kernel: thread ids, buffer row
-  rH, quad start z0, z-PML state column and whether the thread is on a PML
-  warp -- interior warps first (quads plo/4 .. (Z-phi)/4 - 1 of each row),
-  then PML warps (the slab quads, state column 4 * index)."""
-  RH = TY + 1
-  QI, QP = (Z - plo - phi) // 4, (plo + phi) // 4
-  lq = plo // 4
-  nwi = (RH * QI + 31) // 32
-  nwp = (RH * QP + 31) // 32
-  it = np.arange(32 * nwi)
-  thr_i, rH_i = it, it // QI
-  z0_i = 4 * (lq + it % QI)
-  if QP:
-    ip = np.arange(32 * nwp)
-    qi = ip % QP
-    thr_p, rH_p = 32 * nwi + ip, ip // QP
-    z0_p = 4 * np.where(qi < lq, qi, Z // 4 - QP + qi)
-    col_p = 4 * qi
+def lean_split(Z, plo, phi, esz):
+  """The bank-conflict-free item mapping of ``lean_item`` applies."""
+  return esz == 4 and Z == 64 and plo + phi <= 32
+
+
+def lean_items(Z, TY, plo, phi, esz=4):
+  """Every compute thread's item in the lean kernels (``lean_item`` in
+  csrc/lean_kernel.cuh) over TY + 1 buffer rows: thread ids, buffer row,
+  quad start z0, z-PML state column, whether the quad is a z-PML quad, and
+  the thread count.  Split mapping (FP32, zz 64, plo + phi <= 32): edge
+  warps hold each row's quads [0, 8 - ph) and [16 - ph, 16) (ph = phi/4),
+  interior warps quads [8 - ph, 16 - ph), 8 lanes per row.  Otherwise
+  interior warps (quads between the slabs, row-major), then z-PML warps."""
+  rows = TY + 1
+  lq, pq, nq = plo // 4, phi // 4, Z // 4
+  if lean_split(Z, plo, phi, esz):
+    ne = (rows + 3) // 4
+    thr = np.arange(32 * 2 * ne)
+    w, j = thr >> 5, thr & 7
+    edge = w < ne
+    rH = 4 * np.where(edge, w, w - ne) + ((thr >> 3) & 3)
+    q = np.where(edge, np.where(j < 8 - pq, j, j + 8), 8 - pq + j)
   else:
-    thr_p = rH_p = z0_p = col_p = np.zeros(0, np.int64)
-  thr = np.concatenate([thr_i, thr_p])
-  rH = np.concatenate([rH_i, rH_p])
-  z0 = np.concatenate([z0_i, z0_p])
-  col = np.concatenate([np.zeros_like(thr_i), col_p])
-  pml = np.concatenate([np.zeros(len(thr_i), bool), np.ones(len(thr_p), bool)])
-  return thr, rH, z0, col, pml, 32 * (nwi + nwp)
+    QI, QP = (Z - plo - phi) // 4, (plo + phi) // 4
+    nwi = (rows * QI + 31) // 32
+    nwp = (rows * QP + 31) // 32
+    thr = np.arange(32 * (nwi + nwp))
+    pw = thr >= 32 * nwi
+    i = np.where(pw, thr - 32 * nwi, thr)
+    Qn = np.where(pw, QP, QI)
+    rH = np.where(Qn > 0, i // np.maximum(Qn, 1), rows)
+    qi = i - rH * Qn
+    q = np.where(pw, np.where(qi < lq, qi, nq - QP + qi), lq + qi)
+  pml = (q < lq) | (q >= nq - pq)
+  col = 4 * np.where(q < lq, q, lq + q - (nq - pq))
+  return thr, rH, 4 * q, np.where(pml, col, 0), pml, len(thr)
 
 
 def lean_h(sm, it, Z, Y, Pp, y0, RH, ieH, ring_e, ring_e1, ring_h, ring_p,
@@ -403,7 +412,7 @@ def one_step_cta(X, Y, Z, plo, phi, TY, S, seg_x, tile, seg, ncomp, src, cover,
 
   Zh = Z // 2
   rpt = ncomp // Zh
-  litems = lean_items(Z, TY, plo, phi) if lean else None
+  litems = lean_items(Z, TY, plo, phi, esz) if lean else None
   y0 = tile * TY
   xs = seg * seg_x
   xe = min(X, xs + seg_x)
@@ -712,7 +721,7 @@ def two_step_cta(X, Y, Z, plo, phi, TY, SA, SB, seg_x, tile, seg, ncomp, cover,
                lambda c, y: tag(kind + c, level, plane, y))
 
   if lean:  # one (buffer row, quad) item per thread over the NR rows
-    lthr, lra, lz0, lcol, lpml, _ = lean_items(Z, NR - 1, plo, phi)
+    lthr, lra, lz0, lcol, lpml, _ = lean_items(Z, NR - 1, plo, phi, esz)
     lys = y0 - 2 + lra
 
   def items(lo, hi, keep):
@@ -1109,23 +1118,36 @@ def test_lean_compute_accesses(X, Y, Z, TY, plo, phi, esz):
   assert checked > 0
 
 
-def test_lean_items_cover_each_quad_once():
-  """Interior and PML warps together hold every (row, quad) of the H phase
-  exactly once, PML items only z-PML quads, and the PML state column of a
-  PML quad is its z-PML column."""
+@pytest.mark.parametrize("esz", [4, 2])
+def test_lean_items_cover_each_quad_once(esz):
+  """Every (row, quad) of the H phase is held exactly once, z-PML quads
+  are exactly the slab quads, and a z-PML quad's state column is its
+  z-PML column; without the split mapping z-PML quads fill whole warps."""
   for Z, TY, plo, phi in [(64, 14, 8, 8), (48, 19, 4, 12), (32, 29, 0, 0),
-                          (64, 14, 12, 0)]:
-    thr, rH, z0, col, pml, n = lean_items(Z, TY, plo, phi)
+                          (64, 14, 12, 0), (64, 14, 0, 0), (64, 28, 16, 16),
+                          (64, 14, 4, 24), (64, 14, 12, 24)]:
+    thr, rH, z0, col, pml, n = lean_items(Z, TY, plo, phi, esz)
     assert n % 32 == 0 and len(np.unique(thr)) == len(thr)
     live = rH < TY + 1
     pairs = set(zip(rH[live].tolist(), z0[live].tolist()))
     assert len(pairs) == live.sum() == (TY + 1) * Z // 4
+    assert (pml[live] == ((z0[live] < plo) | (z0[live] >= Z - phi))).all()
     zp = z0[live & pml]
-    assert ((zp < plo) | (zp >= Z - phi)).all()
     zc = np.where(zp < plo, zp, zp - (Z - phi) + plo)
     assert (zc == col[live & pml]).all()
-    # whole warps of one kind
-    assert len(np.unique(pml.reshape(-1, 32), axis=1)[0]) <= 2
+    if not lean_split(Z, plo, phi, esz):
+      assert len(np.unique(pml.reshape(-1, 32), axis=1)[0]) <= 2
+
+
+@pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (12, 20), (16, 16)])
+def test_split_items_are_free_of_bank_conflicts(plo, phi):
+  """FP32 zz 64: in every group of 8 lanes (one 128-byte pass of a 128-bit
+  shared access) the quads fall in 8 distinct bank groups (quad % 8; rows
+  are 256 bytes), so no quad access of the lean kernels conflicts."""
+  for TY in (14, 13, 12):
+    thr, rH, z0, _, _, _ = lean_items(64, TY, plo, phi, 4)
+    g = ((z0 // 4) % 8).reshape(-1, 8)
+    assert all(len(set(row)) == 8 for row in g.tolist())
 
 
 def test_lean_model_flags_a_planted_mistake():
