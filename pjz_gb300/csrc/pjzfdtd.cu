@@ -56,6 +56,13 @@ size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
 
 }  // namespace
 
+// The resolved launch geometry of a plan (the fields the resolvers set).
+struct LaunchState {
+  int tile_y, seg_x, threads, steps_per_pass, kernel, stages, threads2, stages2,
+      src_ring, src_rows;
+  size_t smem, smem2;
+};
+
 struct pjzfdtd_plan {
   pjzfdtd_problem p;
   int ns = 0;
@@ -87,6 +94,10 @@ struct pjzfdtd_plan {
          off_srcws = 0, bytes = 0;
   int Pp = 0;  // PML state row stride (P rounded up to 4)
   int Yp = 0;  // padded y length of the streamed kernel's absorber copy
+  // When auto selection chose a lean kernel: the streamed plan it replaced
+  // (same workspace layout), which a batch falls back to.
+  bool has_streamed = false;
+  LaunchState streamed = {};
 };
 
 namespace {
@@ -290,8 +301,32 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
   return PJZFDTD_OK;
 }
 
-// Whether auto selection takes the lean kernel where it applies.
-constexpr bool kLeanAuto = false;
+// Whether auto selection takes the lean kernels where they apply (FP32
+// storage; binary16 always runs on them): the two-step kernel when the
+// steps per pass are automatic, else the one-step kernel.
+constexpr bool kLeanAuto = true;
+constexpr bool kLean2Auto = true;
+
+LaunchState save_launch(const pjzfdtd_plan* pl) {
+  return LaunchState{pl->tile_y,   pl->seg_x,   pl->threads,  pl->steps_per_pass,
+                     pl->kernel,   pl->stages,  pl->threads2, pl->stages2,
+                     pl->src_ring, pl->src_rows, pl->smem,    pl->smem2};
+}
+
+void load_launch(pjzfdtd_plan* pl, const LaunchState& s) {
+  pl->tile_y = s.tile_y;
+  pl->seg_x = s.seg_x;
+  pl->threads = s.threads;
+  pl->steps_per_pass = s.steps_per_pass;
+  pl->kernel = s.kernel;
+  pl->stages = s.stages;
+  pl->threads2 = s.threads2;
+  pl->stages2 = s.stages2;
+  pl->src_ring = s.src_ring;
+  pl->src_rows = s.src_rows;
+  pl->smem = s.smem;
+  pl->smem2 = s.smem2;
+}
 // Whether auto selection takes the tall binary16 lean tile where it applies.
 constexpr bool kLeanTallAuto = false;
 
@@ -365,6 +400,21 @@ int32_t resolve_lean2(pjzfdtd_plan* pl) {
   return PJZFDTD_OK;
 }
 
+// Whether the lean two-step kernel takes a plan resolved for the streamed
+// two-step kernel: a compile-time shape of both lean kernels, z-PML slabs of
+// whole quads, no ring-carried source rows, blocks within their bounds.
+bool lean2_applies(const pjzfdtd_plan* pl) {
+  const pjzfdtd_problem& p = pl->p;
+  const int Z = p.zz, ty = pl->tile_y;
+  if (pl->steps_per_pass != 2 || pl->src_ring != 0 || p.pml_lo % 4 != 0 ||
+      p.pml_hi % 4 != 0 || !lean_kernel_ptr(Z, ty, p.storage) ||
+      !lean2_kernel_ptr(Z, ty, p.storage))
+    return false;
+  return lean2_warps(Z, ty, p.pml_lo, p.pml_hi, pl->esz) * 32 + 32 <= kLeanThreads &&
+         lean_warps(Z, ty + 1, p.pml_lo, p.pml_hi, pl->esz) * 32 + 32 <=
+             lean_kernel_threads(Z, ty, p.storage);
+}
+
 // Resolves the CTA tile.  Register-marching kernel: (tile_y + 2) * zz
 // cells, one thread each, at most kMaxThreads threads.
 int32_t resolve_tile(pjzfdtd_plan* pl) {
@@ -408,7 +458,27 @@ int32_t resolve_tile(pjzfdtd_plan* pl) {
   if (pl->p.kernel == 2 || (pl->p.kernel == 0 && Z % 4 == 0 && Z <= zmax)) {
     int32_t rc = resolve_stream(pl);
     if (rc || pl->p.kernel == 2 || !kLeanAuto) return rc;
-    return resolve_lean(pl, false);
+    // Auto: the lean two-step kernel, else the lean one-step kernel, where
+    // they apply; the streamed plan is kept for batches.
+    const LaunchState streamed = save_launch(pl);
+    if (kLean2Auto && pl->p.steps_per_pass == 0 && pl->src_ring == 0) {
+      pl->p.steps_per_pass = 2;
+      rc = resolve_stream(pl);
+      pl->p.steps_per_pass = 0;
+      if (rc == PJZFDTD_OK && lean2_applies(pl) &&
+          resolve_lean(pl, true) == PJZFDTD_OK && resolve_lean2(pl) == PJZFDTD_OK) {
+        pl->has_streamed = true;
+        pl->streamed = streamed;
+        return PJZFDTD_OK;
+      }
+      load_launch(pl, streamed);
+    }
+    if ((rc = resolve_lean(pl, false))) return rc;
+    if (pl->kernel == 3) {
+      pl->has_streamed = true;
+      pl->streamed = streamed;
+    }
+    return PJZFDTD_OK;
   }
   pl->kernel = 1;
   if (pl->p.steps_per_pass == 2)
@@ -1137,6 +1207,21 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
       delete bt;
       return fail(PJZFDTD_ERR_UNSUPPORTED,
                   "plan %d is not a streamed-kernel plan (zz %% 4 == 0 needed)", i);
+    }
+    if (pl->kernel == 3 && !pl->has_streamed) {
+      delete bt;
+      return fail(PJZFDTD_ERR_UNSUPPORTED,
+                  "plan %d runs the lean kernel by request; batches run the "
+                  "streamed kernels (kernel 0 or 2)", i);
+    }
+  }
+  for (int i = 0; i < n; ++i) {
+    pjzfdtd_plan* pl = plans[i];
+    // A lean plan chosen automatically joins on its streamed plan (same
+    // workspace layout) and keeps it from now on.
+    if (pl->kernel == 3) {
+      load_launch(pl, pl->streamed);
+      pl->has_streamed = false;
     }
     bt->plans.push_back(pl);
     bt->off.push_back(o);

@@ -339,9 +339,10 @@ def plane_source_box(source_field: torch.Tensor, source_position: int,
 
 def run_many(plans, inputs):
   """Runs independent plans: as one :class:`Batch` (one launch per time step
-  for all of them) when every plan stores FP32, else one after another
-  (batches run FP32 storage only).  Returns the ``(out, out_h)`` pairs."""
-  if all(p.problem.storage == STORAGE_F32 for p in plans):
+  for all of them) when every plan stores FP32 and none asked for the lean
+  kernel, else one after another (batches run FP32 storage on the streamed
+  kernels).  Returns the ``(out, out_h)`` pairs."""
+  if all(p.problem.storage == STORAGE_F32 and p.problem.kernel != 3 for p in plans):
     return Batch(plans).run(inputs, graph=False)
   return [p.run(**kw) for p, kw in zip(plans, inputs)]
 

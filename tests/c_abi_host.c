@@ -100,7 +100,10 @@ int main(void) {
   int32_t ty, sx, th, spp, kern, st;
   if (pjzfdtd_plan_launch_config(plan, &ty, &sx, &th, &spp, &kern, &st))
     return fail("launch config");
-  if (kern != 2 || spp != 1 || ty <= 0 || th <= 0) return fail("launch values");
+  /* auto: the streamed (2) or, where a compile-time shape applies, the lean
+     (3) kernel */
+  if (kern < 2 || kern > 3 || spp != 1 || ty <= 0 || th <= 0)
+    return fail("launch values");
   printf("ok plan: workspace %zu bytes, %d samples, kernel %d, tile_y %d, "
          "%d threads, %d steps per pass\n", ws, ns, kern, ty, th, spp);
   pjzfdtd_plan_destroy(plan);

@@ -203,3 +203,34 @@ def test_tall_binary16_tile(lib, pml, ok):
   assert cfg["threads"] <= 512 and cfg["threads"] % 32 == 0
   with pytest.raises(ValueError, match="exceeds shared"):
     engine.Plan(**kw)
+
+
+def test_auto_takes_the_lean_kernels_and_batches_fall_back(lib):
+  """FP32 plans with kernel and steps per pass automatic run the lean
+  two-step kernel where its compile-time shape applies (zz 64, tile_y 14),
+  else the lean one-step kernel; a batch takes such a plan on the streamed
+  plan it replaced (same workspace), while a plan that asked for the lean
+  kernel stays out of batches."""
+  Z = 64
+  kw = dict(domain=(40, 56, Z), offset=(0, 0, 0), region=(40, 56, Z), tt=20,
+            dt=0.5, pml_widths=(8, 8), pml_kappa=np.ones((Z, 2)),
+            pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)),
+            source_origin=(6, 0, 0), source_shape=(2, 56, Z), source_ncols=2)
+  auto = engine.Plan(**kw)
+  cfg = auto.launch_config()
+  assert (cfg["kernel"], cfg["steps_per_pass"], cfg["tile_y"]) == (3, 2, 14)
+  one = engine.Plan(**kw, steps_per_pass=1).launch_config()
+  assert (one["kernel"], one["steps_per_pass"]) == (3, 1)
+  streamed = engine.Plan(**kw, kernel=2)
+  ws = auto.workspace_bytes
+  assert ws == streamed.workspace_bytes
+  engine.Batch([auto])
+  cfg = auto.launch_config()
+  assert (cfg["kernel"], cfg["steps_per_pass"]) == (2, 1)
+  assert auto.workspace_bytes == ws
+  with pytest.raises(NotImplementedError, match="lean kernel by request"):
+    engine.Batch([engine.Plan(**kw, kernel=3)])
+  # odd z-PML widths or a y-normal box that rides the ring keep the streamed
+  # kernels
+  odd = dict(kw, pml_widths=(6, 6))
+  assert engine.Plan(**odd).launch_config()["kernel"] == 2
