@@ -75,8 +75,8 @@ typedef enum {
      all arithmetic, source sums and phasor accumulators in FP32: half the
      HBM bytes per cell-update.  fdtdz's use_reduced_precision
      (src/pjz/_field.py:52, pjz's default) selects 16-bit storage; this is
-     that mode.  Served by the lean streamed kernel (kernel 3), one step per
-     launch, zz in {64, 48, 32} and z-PML widths that are multiples of 4. */
+     that mode.  Served by the lean streamed kernels (kernel 3), zz in
+     {64, 48, 32} and z-PML widths that are multiples of 4. */
   PJZFDTD_STORAGE_F16 = 1
 } pjzfdtd_storage;
 
@@ -99,7 +99,12 @@ typedef struct pjzfdtd_problem {
   int32_t steps_per_pass;      /* launch params: time steps per HBM pass, 0 = auto */
   int32_t kernel;              /* launch params: 0 auto, 1 register-marching,
                                   2 bulk-copy streamed (needs zz % 4 == 0),
-                                  3 lean streamed (compile-time zz/tile_y) */
+                                  3 lean streamed (compile-time zz/tile_y).
+                                  Auto takes the lean kernel (two steps per
+                                  pass when steps_per_pass is 0) where its
+                                  shape applies and the source box does not
+                                  ride the streamed ring, else the streamed
+                                  kernel (zz % 4 == 0), else kernel 1. */
   int32_t stages;              /* launch params: streamed ring depth, 0 = auto */
   int32_t warps;               /* launch params: streamed compute warps per CTA,
                                   0 = auto (one row per warp and pass) */
@@ -192,7 +197,9 @@ int32_t pjzfdtd_plan_output_floats(const pjzfdtd_plan* plan, size_t* floats);
    legacy default stream).  This is the batched scheduler for many forward
    and adjoint solves (multi-port S-matrices); pjz runs them as a Python loop
    of `field` calls (src/pjz/_field.py:354-356).  Plans must be streamed
-   (zz % 4 == 0) and outlive the batch. */
+   (zz % 4 == 0) and outlive the batch; a plan that auto selection put on
+   the lean kernel joins on the streamed plan it replaced (same workspace)
+   and keeps it afterwards, and one made with kernel = 3 is refused. */
 typedef struct pjzfdtd_batch pjzfdtd_batch;
 int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
                              pjzfdtd_batch** batch);

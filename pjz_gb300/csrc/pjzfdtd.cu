@@ -226,12 +226,12 @@ int32_t resolve_stream(pjzfdtd_plan* pl) {
         }
     s2 = t2 > 0 ? stream2_stages(t2, Z, P, pl->p.stages) : 0;
     bool use = t2 > 0 && s2 > 0 && StreamGeom(t2, Z, P).bytes(S) <= kSmemBudget;
-    // Auto keeps one step per pass: the two-step kernel moves about half
-    // the HBM bytes per cell-update but issues ~1.3x the instructions per
-    // cell-update, and on GB300 its time is set on the SM side (instruction
-    // latency with 4-5 warps per scheduler), not by HBM (measured on
-    // 512x512x64: 0.192 ms per step with one step per launch, 0.224 ms
-    // with two), so two steps per pass is chosen only on request.
+    // The streamed kernels keep one step per pass when it is automatic: the
+    // streamed two-step kernel moves about half the HBM bytes per
+    // cell-update but issues ~1.3x the instructions, and on GB300 its time
+    // is set on the SM side, not by HBM (512x512x64: 0.192 ms per step with
+    // one step per launch, 0.224 ms with two).  Auto selection takes two
+    // steps per pass on the lean two-step kernel instead (resolve_tile).
     if (spp == 0) use = false;
     if (use) {
       ty = t2;
