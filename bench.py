@@ -12,7 +12,10 @@ Output: one JSON line (rank 0).  ``value`` is device-resident throughput of
 the engine plan; ``e2e`` is the same metric through ``pjz_gb300.field`` with
 host inputs (H2D of epsilon/source and D2H of the complex phasors inside the
 timed region).  ``roofline`` compares the step kernel's algorithmic bytes
-(60 B per cell-update) per launch against the measured HBM copy bandwidth.
+(60 B per cell-update, times the cell-updates of one launch: two per cell
+for a two-step launch) per launch time against the measured HBM copy
+bandwidth; ``traffic`` is the DRAM bytes ncu counted for one launch, below
+the algorithmic bytes when a launch advances two steps.
 ``--impl reference`` times the CPU path (the oracle's C Yee transcription
 on all host cores; the reference engine is CUDA-only and not available).
 The native line's ``cpu_baseline`` also carries ``torch_eager``: the same
@@ -319,14 +322,19 @@ def run_native(args):
   plan.run(**run_args, out=out, steps=(1, 1 + nl))
   k1.record(stream)
   torch.cuda.synchronize()
-  # Each launch reads and writes the state once, whether it advances one
-  # step or two (temporal blocking): 60 B per cell per launch.
+  # Algorithmic bytes are 60 B per cell-update; a two-step launch
+  # (temporal blocking) performs two cell-updates per cell while it reads
+  # and writes the state once, so its DRAM traffic (`traffic`) falls below
+  # its algorithmic bytes.  `state_gbs` is the state actually streamed (60 B
+  # per cell per launch).
   cfg0 = plan.launch_config()
   launches = plan.step_launches(1, 1 + nl)
   launch_ms = k0.elapsed_time(k1) / launches
   cells_per_launch = int(np.prod(wl.domain))
-  achieved = BYTES_PER_CELL * cells_per_launch / (launch_ms / 1e3) / 1e9
-  effective = BYTES_PER_CELL * cells_per_launch * nl / launches / (launch_ms / 1e3) / 1e9
+  steps_per_launch = nl / launches
+  alg_bytes = BYTES_PER_CELL * cells_per_launch * steps_per_launch
+  achieved = alg_bytes / (launch_ms / 1e3) / 1e9
+  state_gbs = BYTES_PER_CELL * cells_per_launch / (launch_ms / 1e3) / 1e9
   peak, peak_kind = _peaks()
   kname = {(3, 2): "yee_lean2", (3, 1): "yee_lean", (2, 2): "yee_stream2",
            (2, 1): "yee_stream"}.get((cfg0["kernel"], cfg0["steps_per_pass"]),
@@ -336,9 +344,9 @@ def run_native(args):
               "unit": "GB/s", "frac": achieved / peak,
               "peak_source": f"hbm_gbs of {peak_kind}",
               "kernel": f"{kname}_kernel",
-              "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells_per_launch,
-              "steps_per_launch": nl / launches,
-              "effective_gbs_per_step": effective,
+              "algorithmic_bytes_per_launch": alg_bytes,
+              "steps_per_launch": steps_per_launch,
+              "state_gbs": state_gbs,
               "launch_ms": launch_ms,
               "traffic": None if bpc is None else bpc * cells_per_launch}
 
