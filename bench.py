@@ -162,8 +162,10 @@ def _profile_traffic(name):
   try:
     with open(path) as f:
       d = json.load(f)
-    return float(d.get("dram_bytes_per_cell_per_launch",
-                       d["dram_bytes_per_cell_update"])), d
+    v = d.get("dram_bytes_per_cell_per_launch")
+    if v is None:
+      v = d["dram_bytes_per_cell_update"]
+    return float(v), d
   except (OSError, KeyError, ValueError):
     return None, None
 
