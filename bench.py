@@ -352,10 +352,6 @@ def run_native(args):
               "launch_ms": launch_ms,
               "traffic": None if bpc is None else bpc * cells_per_launch}
 
-  f16 = None
-  if args.workload == "c1" and not args.no_f16:
-    f16 = f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells)
-
   e2e = None
   if not args.no_e2e:
     eps_h = torch.as_tensor(wl.epsilon).pin_memory()
@@ -371,6 +367,7 @@ def run_native(args):
                             wl.source_pos, sp)
       host.copy_(res, non_blocking=True)
     barrier()
+    clk_e = Clocks(local, _clock_path(f"e2e_{rank}"))
     t0 = time.perf_counter()
     for _ in range(args.steps):
       res = pjz_gb300.field(eps_h.to(dev, non_blocking=True),
@@ -382,7 +379,12 @@ def run_native(args):
     e2e = {"value": world * cells / t_e2e / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": eps_h.numel() * 4 + src_h.numel() * 4,
            "d2h_bytes_per_step": host.numel() * host.element_size(),
-           "ms_per_step": t_e2e * 1e3}
+           "ms_per_step": t_e2e * 1e3, "clocks": clk_e.stop()}
+    del res
+
+  f16 = None
+  if args.workload == "c1" and not args.no_f16:
+    f16 = f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells)
 
   cpu = None
   if rank == 0 and not args.no_cpu:
