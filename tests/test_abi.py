@@ -185,17 +185,17 @@ def test_binary16_plans_stay_out_of_batches(lib):
 
 
 @pytest.mark.parametrize("pml,ok", [((0, 0), True), ((8, 8), True), ((4, 12), True),
-                                    ((12, 12), False)])
+                                    ((12, 12), True), ((6, 6), False)])
 def test_tall_binary16_tile(lib, pml, ok):
-  """tile_y=28 at zz 64 with binary16 storage takes the tall lean tile (16
-  warps at most: z-PML slabs up to 16 cells wide); wider slabs need more
-  warps than its block bound and are refused.  FP32 has no such tile."""
+  """tile_y=28 at zz 64 with binary16 storage takes the tall lean tile (two
+  rows per warp, 15 compute warps for any slab widths); slabs that are not
+  whole quads are refused.  FP32 has no such tile."""
   Z = 64
   kw = dict(domain=(20, 61, Z), offset=(0, 0, 0), region=(20, 61, Z), tt=20,
             dt=0.5, pml_widths=pml, pml_kappa=np.ones((Z, 2)),
             pml_sigma=np.zeros((Z, 2)), pml_alpha=np.zeros((Z, 2)), tile_y=28)
   if not ok:
-    with pytest.raises(NotImplementedError, match="warps"):
+    with pytest.raises(NotImplementedError, match="multiples of 4"):
       engine.Plan(**kw, storage=engine.STORAGE_F16)
     return
   cfg = engine.Plan(**kw, storage=engine.STORAGE_F16).launch_config()

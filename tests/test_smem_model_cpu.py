@@ -242,8 +242,13 @@ def pml_columns(Z, plo, phi):
 
 
 def lean_split(Z, plo, phi, esz):
-  """The bank-conflict-free item mapping of ``lean_item`` applies."""
+  """The bank-conflict-free split mapping of ``lean_item`` applies."""
   return esz == 4 and Z == 64 and plo + phi <= 32
+
+
+def lean_rows(Z, esz):
+  """The whole-row mapping of ``lean_item`` applies (binary16, zz 64)."""
+  return esz == 2 and Z == 64
 
 
 def lean_items(Z, TY, plo, phi, esz=4):
@@ -263,6 +268,9 @@ def lean_items(Z, TY, plo, phi, esz=4):
     edge = w < ne
     rH = 4 * np.where(edge, w, w - ne) + ((thr >> 3) & 3)
     q = np.where(edge, np.where(j < 8 - pq, j, j + 8), 8 - pq + j)
+  elif lean_rows(Z, esz):
+    thr = np.arange(32 * ((rows + 1) // 2))
+    rH, q = thr >> 4, thr & 15
   else:
     QI, QP = (Z - plo - phi) // 4, (plo + phi) // 4
     nwi = (rows * QI + 31) // 32
@@ -1135,8 +1143,19 @@ def test_lean_items_cover_each_quad_once(esz):
     zp = z0[live & pml]
     zc = np.where(zp < plo, zp, zp - (Z - phi) + plo)
     assert (zc == col[live & pml]).all()
-    if not lean_split(Z, plo, phi, esz):
+    if not lean_split(Z, plo, phi, esz) and not lean_rows(Z, esz):
       assert len(np.unique(pml.reshape(-1, 32), axis=1)[0]) <= 2
+
+
+@pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (12, 20), (16, 16)])
+def test_row_items_are_free_of_bank_conflicts_in_binary16(plo, phi):
+  """Binary16 zz 64: every group of 16 lanes (one 128-byte pass of a 64-bit
+  shared access) holds 16 distinct bank pairs (quad % 16; rows are 128
+  bytes)."""
+  for TY in (14, 13, 28):
+    thr, rH, z0, _, _, _ = lean_items(64, TY, plo, phi, 2)
+    g = ((z0 // 4) % 16).reshape(-1, 16)
+    assert all(len(set(row)) == 16 for row in g.tolist())
 
 
 @pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (12, 20), (16, 16)])
