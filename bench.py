@@ -459,8 +459,8 @@ def f16_leg(args, wl, eps, src, stream, barrier, maxed, world, cells):
   peak, peak_kind = _peaks()
   cfg = plan.launch_config()
   bpc = None
-  if cfg["kernel"] == 3 and cfg["steps_per_pass"] == 1 and cfg["tile_y"] == 14:
-    bpc, _ = _profile_traffic(f"yee_lean_f16_{args.workload}")
+  if cfg["kernel"] == 3 and cfg["steps_per_pass"] == 1:
+    bpc, _ = _profile_traffic(f"yee_lean_f16_ty{cfg['tile_y']}_{args.workload}")
   return {"value": world * cells / (ms / 1e3) / 1e9, "unit": UNIT,
           "ms_per_step": ms, "dtype": "binary16 storage, f32 arithmetic",
           "launch": cfg,

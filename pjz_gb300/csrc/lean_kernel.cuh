@@ -198,7 +198,8 @@ struct Quad<__half> {
 // for these zz with 4 ring stages (zz 32 with a 16-cell z-PML: 28).
 #define PJZ_LEAN_SHAPES(X_) X_(64, 14) X_(48, 19) X_(32, 29) X_(32, 28)
 // Taller binary16 tiles (half the shared memory per row): 16 warps per CTA
-// hide more latency than 9 and the y halo is half as large per cell.
+// hide more latency than 9 and the y halo is half as large per cell
+// (auto selection takes them for one step per pass).
 #define PJZ_LEAN_SHAPES_F16(X_) X_(64, 28)
 
 // Block bound of a lean kernel instantiation: one CTA per SM (the ring and

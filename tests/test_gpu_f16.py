@@ -35,7 +35,7 @@ def test_f16_snapshots_bit_exact(native, Z, TY, pml, src):
                         pml=pml, src=src, src_pos=5 if src == "z" else 7,
                         tt=24, steps=(9, 24, 4))
   want = oracle.run(**oracle_kwargs(case), storage="f16")["out"]
-  got, _, _ = gpu16(case, seg_x=6)
+  got, _, _ = gpu16(case, seg_x=6, tile_y=TY)
   assert np.array_equal(got, want), np.abs(got - want).max()
 
 
