@@ -57,7 +57,11 @@ __host__ __device__ inline int lean_quads_pml(int plo, int phi) {
 // lanes at a time and quad q of a 128-byte row sits in bank pair q % 16,
 // so conflict-free passes need whole rows: lanes 16 h .. 16 h + 15 of a
 // warp hold the 16 quads of one row, and every warp branches per lane on
-// the z-PML update.
+// the z-PML update.  zz 32 (either storage) takes whole rows too, row-major
+// (8 quads per row, 4 rows per warp): consecutive lanes hold consecutive
+// 16-byte (8-byte) pieces of shared memory, which no pass repeats a bank
+// of, where the split of interior and slab quads left every pass 2-way
+// conflicted.
 //
 // Otherwise: interior warps first (the quads between the slabs, row-major),
 // then z-PML warps (the slab quads), so the z-PML branch is warp-uniform.
@@ -72,11 +76,13 @@ __host__ __device__ inline bool lean_split(int Z, int plo, int phi, int esz) {
   return esz == 4 && Z == 64 && plo + phi <= 32;
 }
 
-__host__ __device__ inline bool lean_rows(int Z, int esz) { return esz == 2 && Z == 64; }
+__host__ __device__ inline bool lean_rows(int Z, int esz) {
+  return (esz == 2 && Z == 64) || Z == 32;
+}
 
 __host__ __device__ inline int lean_warps(int Z, int rows, int plo, int phi, int esz) {
   if (lean_split(Z, plo, phi, esz)) return 2 * ((rows + 3) / 4);
-  if (lean_rows(Z, esz)) return (rows + 1) / 2;
+  if (lean_rows(Z, esz)) return (rows * (Z / 4) + 31) / 32;
   return (rows * lean_quads_interior(Z, plo, phi) + 31) / 32 +
          (rows * lean_quads_pml(plo, phi) + 31) / 32;
 }
@@ -93,8 +99,8 @@ __host__ __device__ inline LeanItem lean_item(int tid, int Z, int rows, int plo,
     it.row = 4 * (edge ? w : w - ne) + ((tid >> 3) & 3);
     q = edge ? (j < 8 - pq ? j : j + 8) : 8 - pq + j;
   } else if (lean_rows(Z, esz)) {
-    it.row = tid >> 4;
-    q = tid & 15;
+    it.row = tid / nq;  // nq is 16 or 8
+    q = tid - it.row * nq;
   } else {
     const int QI = lean_quads_interior(Z, plo, phi), QP = lean_quads_pml(plo, phi);
     const int nwi = (rows * QI + 31) / 32;

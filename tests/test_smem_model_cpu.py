@@ -247,8 +247,9 @@ def lean_split(Z, plo, phi, esz):
 
 
 def lean_rows(Z, esz):
-  """The whole-row mapping of ``lean_item`` applies (binary16, zz 64)."""
-  return esz == 2 and Z == 64
+  """The whole-row mapping of ``lean_item`` applies (binary16 zz 64, or
+  zz 32)."""
+  return (esz == 2 and Z == 64) or Z == 32
 
 
 def lean_items(Z, TY, plo, phi, esz=4):
@@ -269,8 +270,8 @@ def lean_items(Z, TY, plo, phi, esz=4):
     rH = 4 * np.where(edge, w, w - ne) + ((thr >> 3) & 3)
     q = np.where(edge, np.where(j < 8 - pq, j, j + 8), 8 - pq + j)
   elif lean_rows(Z, esz):
-    thr = np.arange(32 * ((rows + 1) // 2))
-    rH, q = thr >> 4, thr & 15
+    thr = np.arange(32 * ((rows * nq + 31) // 32))
+    rH, q = thr // nq, thr % nq
   else:
     QI, QP = (Z - plo - phi) // 4, (plo + phi) // 4
     nwi = (rows * QI + 31) // 32
@@ -1156,6 +1157,21 @@ def test_row_items_are_free_of_bank_conflicts_in_binary16(plo, phi):
     thr, rH, z0, _, _, _ = lean_items(64, TY, plo, phi, 2)
     g = ((z0 // 4) % 16).reshape(-1, 16)
     assert all(len(set(row)) == 16 for row in g.tolist())
+
+
+@pytest.mark.parametrize("esz", [4, 2])
+@pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (16, 16)])
+def test_zz32_rows_are_free_of_bank_conflicts(esz, plo, phi):
+  """zz 32: lanes hold consecutive quads row-major, so each pass (8 lanes
+  of 16 bytes for FP32, 16 lanes of 8 bytes for binary16) covers 128
+  contiguous bytes of a region: distinct banks."""
+  quad = 4 * esz              # bytes per quad access
+  lanes = 128 // quad          # lanes per 128-byte pass
+  for TY in (29, 28, 5):
+    thr, rH, z0, _, _, _ = lean_items(32, TY, plo, phi, esz)
+    off = (rH * 32 + z0) * esz  # byte offset of the quad in a row-major region
+    group = (off // quad) % lanes  # the quad's group of banks
+    assert all(len(set(row)) == lanes for row in group.reshape(-1, lanes).tolist())
 
 
 @pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (12, 20), (16, 16)])
