@@ -100,11 +100,11 @@ typedef struct pjzfdtd_problem {
   int32_t kernel;              /* launch params: 0 auto, 1 register-marching,
                                   2 bulk-copy streamed (needs zz % 4 == 0),
                                   3 lean streamed (compile-time zz/tile_y).
-                                  Auto takes the lean kernel (two steps per
-                                  pass when steps_per_pass is 0) where its
-                                  shape applies and the source box does not
-                                  ride the streamed ring, else the streamed
-                                  kernel (zz % 4 == 0), else kernel 1. */
+                                  Auto (FP32): the lean kernel at zz 64 (two
+                                  steps per pass when steps_per_pass is 0)
+                                  when the source box does not ride the
+                                  streamed ring, else the streamed kernel
+                                  (zz % 4 == 0), else kernel 1. */
   int32_t stages;              /* launch params: streamed ring depth, 0 = auto */
   int32_t warps;               /* launch params: streamed compute warps per CTA,
                                   0 = auto (one row per warp and pass) */
