@@ -53,15 +53,14 @@ __host__ __device__ inline int lean_quads_pml(int plo, int phi) {
 // access is free of bank conflicts; edge warps branch per lane on the
 // z-PML update.
 //
-// Row mapping (binary16 storage, zz 64): a 64-bit access is served 16
-// lanes at a time and quad q of a 128-byte row sits in bank pair q % 16,
-// so conflict-free passes need whole rows: lanes 16 h .. 16 h + 15 of a
-// warp hold the 16 quads of one row, and every warp branches per lane on
-// the z-PML update.  zz 32 (either storage) takes whole rows too, row-major
-// (8 quads per row, 4 rows per warp): consecutive lanes hold consecutive
-// 16-byte (8-byte) pieces of shared memory, which no pass repeats a bank
-// of, where the split of interior and slab quads left every pass 2-way
-// conflicted.
+// Row-major mapping (binary16 storage, or zz 32): consecutive lanes hold
+// consecutive quads of the row-major (row, quad) order, i.e. consecutive
+// 8-byte (binary16) or 16-byte (FP32) pieces of every shared region, so no
+// pass (16 lanes of 8 bytes, 8 lanes of 16 bytes) repeats a bank; every
+// warp branches per lane on the z-PML update.  For binary16 at zz 64 a
+// 64-bit pass must cover a whole 128-byte row to be conflict-free, which
+// no split of interior and slab quads gives; at zz 32 that split left
+// every pass 2-way conflicted.
 //
 // Otherwise: interior warps first (the quads between the slabs, row-major),
 // then z-PML warps (the slab quads), so the z-PML branch is warp-uniform.
@@ -77,7 +76,7 @@ __host__ __device__ inline bool lean_split(int Z, int plo, int phi, int esz) {
 }
 
 __host__ __device__ inline bool lean_rows(int Z, int esz) {
-  return (esz == 2 && Z == 64) || Z == 32;
+  return esz == 2 || Z == 32;
 }
 
 __host__ __device__ inline int lean_warps(int Z, int rows, int plo, int phi, int esz) {
@@ -99,7 +98,7 @@ __host__ __device__ inline LeanItem lean_item(int tid, int Z, int rows, int plo,
     it.row = 4 * (edge ? w : w - ne) + ((tid >> 3) & 3);
     q = edge ? (j < 8 - pq ? j : j + 8) : 8 - pq + j;
   } else if (lean_rows(Z, esz)) {
-    it.row = tid / nq;  // nq is 16 or 8
+    it.row = tid / nq;
     q = tid - it.row * nq;
   } else {
     const int QI = lean_quads_interior(Z, plo, phi), QP = lean_quads_pml(plo, phi);

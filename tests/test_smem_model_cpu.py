@@ -247,9 +247,8 @@ def lean_split(Z, plo, phi, esz):
 
 
 def lean_rows(Z, esz):
-  """The whole-row mapping of ``lean_item`` applies (binary16 zz 64, or
-  zz 32)."""
-  return (esz == 2 and Z == 64) or Z == 32
+  """The row-major mapping of ``lean_item`` applies (binary16, or zz 32)."""
+  return esz == 2 or Z == 32
 
 
 def lean_items(Z, TY, plo, phi, esz=4):
@@ -1159,17 +1158,17 @@ def test_row_items_are_free_of_bank_conflicts_in_binary16(plo, phi):
     assert all(len(set(row)) == 16 for row in g.tolist())
 
 
-@pytest.mark.parametrize("esz", [4, 2])
+@pytest.mark.parametrize("Z,esz", [(32, 4), (32, 2), (48, 2), (64, 2)])
 @pytest.mark.parametrize("plo,phi", [(8, 8), (0, 0), (4, 12), (16, 16)])
-def test_zz32_rows_are_free_of_bank_conflicts(esz, plo, phi):
-  """zz 32: lanes hold consecutive quads row-major, so each pass (8 lanes
-  of 16 bytes for FP32, 16 lanes of 8 bytes for binary16) covers 128
-  contiguous bytes of a region: distinct banks."""
+def test_row_major_items_are_free_of_bank_conflicts(Z, esz, plo, phi):
+  """Row-major items (zz 32, binary16): lanes hold consecutive quads, so
+  each pass (8 lanes of 16 bytes for FP32, 16 lanes of 8 bytes for
+  binary16) covers 128 contiguous bytes of a region: distinct banks."""
   quad = 4 * esz              # bytes per quad access
   lanes = 128 // quad          # lanes per 128-byte pass
-  for TY in (29, 28, 5):
-    thr, rH, z0, _, _, _ = lean_items(32, TY, plo, phi, esz)
-    off = (rH * 32 + z0) * esz  # byte offset of the quad in a row-major region
+  for TY in (29, 28, 19, 5):
+    thr, rH, z0, _, _, _ = lean_items(Z, TY, plo, phi, esz)
+    off = (rH * Z + z0) * esz  # byte offset of the quad in a row-major region
     group = (off // quad) % lanes  # the quad's group of banks
     assert all(len(set(row)) == lanes for row in group.reshape(-1, lanes).tolist())
 
