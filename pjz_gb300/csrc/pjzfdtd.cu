@@ -347,9 +347,9 @@ int32_t resolve_lean(pjzfdtd_plan* pl, bool required) {
     if (!required) return PJZFDTD_OK;
     return fail(PJZFDTD_ERR_UNSUPPORTED,
                 "the lean kernel needs (zz, tile_y) in {(64, 14), (48, 19), "
-                "(32, 29), (32, 28)} (got (%d, %d)), one step per launch and "
-                "z-PML widths "
-                "that are multiples of 4 (got %d, %d)",
+                "(32, 29), (32, 28)}, or (64, 28) with binary16 storage (got "
+                "(%d, %d)), and z-PML widths that are multiples of 4 (got %d, "
+                "%d)",
                 Z, ty, p.pml_lo, p.pml_hi);
   }
   const int warps = lean_warps(Z, ty + 1, p.pml_lo, p.pml_hi, pl->esz);
