@@ -500,12 +500,13 @@ PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l
 // component, the same for every row.
 PJZ_HD void render_phase_cut_fractions(const RenderArgs& a, const RenderSmem& s,
                                        int tid, int nthr) {
-  const int per = kRenderCutCap * a.ll;
-  for (int t = tid; t < 3 * per; t += nthr) {
-    const int c = t >= 2 * per ? 2 : (t >= per ? 1 : 0), r = t - c * per;
-    const int j = r / a.ll, l = r - j * a.ll;
-    if (j < s.ncut[c])
-      render_occupancy(a, s.pos, c, l, s.cut[c * a.zz + j], &s.cutf[t], &s.cutm[t]);
+  for (int c = 0; c < 3; ++c) {
+    const int nc = s.ncut[c] < kRenderCutCap ? s.ncut[c] : kRenderCutCap;
+    for (int t = tid; t < nc * a.ll; t += nthr) {
+      const int j = t / a.ll, l = t - j * a.ll;
+      const int k = (c * kRenderCutCap + j) * a.ll + l;
+      render_occupancy(a, s.pos, c, l, s.cut[c * a.zz + j], &s.cutf[k], &s.cutm[k]);
+    }
   }
 }
 
@@ -514,14 +515,16 @@ PJZ_HD void render_phase_cut_fractions(const RenderArgs& a, const RenderSmem& s,
 // statistics, from the tabulated occupancy.
 PJZ_HD void render_phase_cut_values(const RenderArgs& a, const RenderSmem& s,
                                     int ny, int tid, int nthr) {
-  const int per = kRenderCutCap * kRenderTileY;
-  for (int t = tid; t < 3 * per; t += nthr) {
-    const int c = t >= 2 * per ? 2 : (t >= per ? 1 : 0), r = t - c * per;
-    const int j = r / kRenderTileY, yl = r % kRenderTileY;
-    const int cy = c * kRenderTileY + yl;
-    if (j < s.ncut[c] && yl < ny && s.yfin[cy]) {
-      const int k = (c * kRenderCutCap + j) * a.ll;
-      s.cutv[t] = render_value_tab(a, c, s.st + cy * a.ll, s.cutf + k, s.cutm + k);
+  for (int c = 0; c < 3; ++c) {
+    const int nc = s.ncut[c] < kRenderCutCap ? s.ncut[c] : kRenderCutCap;
+    for (int t = tid; t < nc * kRenderTileY; t += nthr) {
+      const int j = t / kRenderTileY, yl = t % kRenderTileY;
+      const int cy = c * kRenderTileY + yl;
+      if (yl < ny && s.yfin[cy]) {
+        const int k = (c * kRenderCutCap + j) * a.ll;
+        s.cutv[c * kRenderCutCap * kRenderTileY + t] =
+            render_value_tab(a, c, s.st + cy * a.ll, s.cutf + k, s.cutm + k);
+      }
     }
   }
 }
