@@ -119,16 +119,11 @@ PJZ_HD int render_div(int t, uint32_t magic) {
 // the pixel offsets u [2m], the interface positions [kRenderMaxLayers], and
 // per component the z cells an interface cuts [3][zz] (int) and their
 // count [4] (int).
-// Interface-cut cells per component whose values are computed ahead of the
-// output phase (nondecreasing positions cut at most kRenderMaxLayers - 1).
-constexpr int kRenderCutCap = 16;
-
 PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group) {
   return 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
          3 * kRenderTileY +
          2 * (size_t)group * render_patch_rows(m) * render_patch_cols(m) + 2 * m +
-         kRenderMaxLayers + 3 * (size_t)zz + 4 + 3 * (size_t)zz +
-         6 * (size_t)kRenderCutCap * ll + 3 * (size_t)kRenderCutCap * kRenderTileY;
+         kRenderMaxLayers + 3 * (size_t)zz + 4;
 }
 
 // The regions of one CTA's shared memory (render_smem_floats floats).
@@ -142,12 +137,7 @@ struct RenderSmem {
   float* u;         // [2m]
   float* pos;       // [kRenderMaxLayers]
   int* cut;         // [3][zz]: z cells no single layer fills
-  int* ncut;        // [4]: their number per component; [3] = 1 when a row's
-                    // statistics are not all finite
-  int* cutidx;      // [3][zz]: index of z in cut, or -1
-  float* cutf;      // [3][kRenderCutCap][ll]: fractions of the first cut cells
-  float* cutm;      // [3][kRenderCutCap][ll]: their midpoint offsets
-  float* cutv;      // [3][kRenderCutCap][kRenderTileY]: their values per row
+  int* ncut;        // [4]: their number per component
   float* end;
 };
 
@@ -165,11 +155,7 @@ PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m, int group) {
   s.pos = s.u + 2 * m;
   s.cut = reinterpret_cast<int*>(s.pos + kRenderMaxLayers);
   s.ncut = s.cut + 3 * zz;
-  s.cutidx = s.ncut + 4;
-  s.cutf = reinterpret_cast<float*>(s.cutidx + 3 * zz);
-  s.cutm = s.cutf + 3 * kRenderCutCap * ll;
-  s.cutv = s.cutm + 3 * kRenderCutCap * ll;
-  s.end = s.cutv + 3 * kRenderCutCap * kRenderTileY;
+  s.end = reinterpret_cast<float*>(s.ncut + 4);
   return s;
 }
 
@@ -279,22 +265,6 @@ PJZ_HD float render_value(const RenderArgs& a, const float* pos, int c,
   return render_mix(a, c, avg, inv, gx, gy, gz);
 }
 
-// render_value from tabulated fractions `fr` and midpoint offsets `md` of
-// the cell (one per layer): the same operations in the same order.
-PJZ_HD float render_value_tab(const RenderArgs& a, int c, const WindowStats* st,
-                              const float* fr, const float* md) {
-  float avg = 0.f, inv = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int l = 0; l < a.ll; ++l) {
-    const float f = fr[l];
-    avg += st[l].mean * f;
-    inv += st[l].inv * f;
-    gx += st[l].gx * f;
-    gy += st[l].gy * f;
-    gz += st[l].mean * f * md[l];
-  }
-  return render_mix(a, c, avg, inv, gx, gy, gz);
-}
-
 // Value of a z cell that one layer fills: render_value with that layer's
 // fraction 1, midpoint offset 0 and every other fraction 0 (each sum then
 // holds that layer's term alone, and the z moment +0).
@@ -375,7 +345,6 @@ PJZ_HD void render_phase_setup(const RenderArgs& a, const RenderSmem& s, int tid
   }
   for (int t = tid; t < 2 * a.m; t += nthr) s.u[t] = render_u(a, t);
   for (int t = tid; t < 3 * kRenderTileY; t += nthr) s.yfin[t] = 1;
-  if (tid == 0) s.ncut[3] = 0;
 }
 
 // Phase 2 (after the positions are in shared memory): the filling layer of
@@ -405,9 +374,7 @@ __device__ __forceinline__ void render_phase_cuts(const RenderArgs& a,
     const int z = z0 + lane;
     const bool f = z < a.zz && s.owner[c * a.zz + z] < 0;
     const unsigned m = __ballot_sync(0xffffffffu, f);
-    const int j = n + __popc(m & ((1u << lane) - 1u));
-    if (f) s.cut[c * a.zz + j] = z;
-    if (z < a.zz) s.cutidx[c * a.zz + z] = f ? j : -1;
+    if (f) s.cut[c * a.zz + n + __popc(m & ((1u << lane) - 1u))] = z;
     n += __popc(m);
   }
   if (lane == 0) s.ncut[c] = n;
@@ -417,11 +384,8 @@ inline void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
                               int nthr) {
   for (int c = tid; c < 3; c += nthr) {
     int n = 0;
-    for (int z = 0; z < a.zz; ++z) {
-      const bool f = s.owner[c * a.zz + z] < 0;
-      s.cutidx[c * a.zz + z] = f ? n : -1;
-      if (f) s.cut[c * a.zz + n++] = z;
-    }
+    for (int z = 0; z < a.zz; ++z)
+      if (s.owner[c * a.zz + z] < 0) s.cut[c * a.zz + n++] = z;
     s.ncut[c] = n;
   }
 }
@@ -488,62 +452,17 @@ PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l
     const int i = cy * a.ll + l0 + g;
     s.st[i] = render_window(a, c, yl, s.pf + g * np1, s.pinv + g * np1, pc, s.u);
     s.ival[i] = render_interior(a, c, s.st[i]);
-    if (!render_finite(s.st[i])) {  // any writer stores the same values
-      s.yfin[cy] = 0;
-      s.ncut[3] = 1;
-    }
+    if (!render_finite(s.st[i])) s.yfin[cy] = 0;  // any writer stores 0
   }
 }
 
-// Beside the first group's phase 5: the occupancy (fraction, midpoint
-// offset) of every layer in the first kRenderCutCap cut cells of each
-// component, the same for every row.
-PJZ_HD void render_phase_cut_fractions(const RenderArgs& a, const RenderSmem& s,
-                                       int tid, int nthr) {
-  for (int c = 0; c < 3; ++c) {
-    const int nc = s.ncut[c] < kRenderCutCap ? s.ncut[c] : kRenderCutCap;
-    for (int t = tid; t < nc * a.ll; t += nthr) {
-      const int j = t / a.ll, l = t - j * a.ll;
-      const int k = (c * kRenderCutCap + j) * a.ll + l;
-      render_occupancy(a, s.pos, c, l, s.cut[c * a.zz + j], &s.cutf[k], &s.cutm[k]);
-    }
-  }
-}
-
-// Phase 6 (after the last group's windows): the full mix of the first
-// kRenderCutCap cut cells of each component for every row with finite
-// statistics, from the tabulated occupancy.
-PJZ_HD void render_phase_cut_values(const RenderArgs& a, const RenderSmem& s,
-                                    int ny, int tid, int nthr) {
-  for (int c = 0; c < 3; ++c) {
-    const int nc = s.ncut[c] < kRenderCutCap ? s.ncut[c] : kRenderCutCap;
-    for (int t = tid; t < nc * kRenderTileY; t += nthr) {
-      const int j = t / kRenderTileY, yl = t % kRenderTileY;
-      const int cy = c * kRenderTileY + yl;
-      if (yl < ny && s.yfin[cy]) {
-        const int k = (c * kRenderCutCap + j) * a.ll;
-        s.cutv[c * kRenderCutCap * kRenderTileY + t] =
-            render_value_tab(a, c, s.st + cy * a.ll, s.cutf + k, s.cutm + k);
-      }
-    }
-  }
-}
-
-// Value of an interface-cut cell z of component c at tile row yl (finite
-// statistics) as tabulated by phase 6; 0 past the cap (phase 8 writes it).
-PJZ_HD float render_cut_value(const RenderArgs& a, const RenderSmem& s, int c, int yl,
-                              int z) {
-  const int j = s.cutidx[c * a.zz + z];
-  return j < kRenderCutCap ? s.cutv[(c * kRenderCutCap + j) * kRenderTileY + yl] : 0.f;
-}
-
-// Phase 7: outputs.  With zz % 4 == 0 and a 16-byte aligned output each
-// thread writes four consecutive z cells at a time, z fastest over the
-// CTA's threads: coalesced 16-byte stores.  Otherwise warp `w` takes whole
-// (component, y) rows, lane `lane` along z.  Cells one layer fills copy its
-// value and interface-cut cells take phase 6's values; cut cells past the
-// cap and rows whose statistics are not all finite get a placeholder that
-// phase 8 overwrites.
+// Phase 6: outputs of the cells one layer fills.  With zz % 4 == 0 and a
+// 16-byte aligned output each thread writes four consecutive z cells at a
+// time (interface-cut cells among them get a placeholder that phase 7
+// overwrites after a barrier), z fastest over the CTA's threads: coalesced
+// 16-byte stores.  Otherwise warp `w` takes whole (component, y) rows, lane
+// `lane` along z, skipping cut cells.  A row whose statistics are not all
+// finite takes the full mix at every z here.
 PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
                              int y0, int ny, int w, int nw, int lane,
                              float* out) {
@@ -554,14 +473,17 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
       for (int t = tid; t < ny * zq; t += nthr) {
         const int yl = render_div(t, a.zq_magic), z = 4 * (t - yl * zq);
         const int cy = c * kRenderTileY + yl;
-        float v[4] = {0.f, 0.f, 0.f, 0.f};
+        float v[4];
         if (s.yfin[cy]) {
           const float* iv = s.ival + cy * a.ll;
           int o[4];
           render_owner4(s.owner + c * a.zz + z, o);
 #pragma unroll
+          for (int j = 0; j < 4; ++j) v[j] = o[j] >= 0 ? iv[o[j]] : 0.f;
+        } else {
+#pragma unroll
           for (int j = 0; j < 4; ++j)
-            v[j] = o[j] >= 0 ? iv[o[j]] : render_cut_value(a, s, c, yl, z + j);
+            v[j] = render_value(a, s.pos, c, s.st + cy * a.ll, z + j);
         }
         render_store4(out + render_out_index(a, c, x, y0 + yl, z), v);
       }
@@ -570,35 +492,31 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
   for (int c = 0; c < 3; ++c)
     for (int yl = w; yl < ny; yl += nw) {
       const int cy = c * kRenderTileY + yl;
+      const WindowStats* st = s.st + cy * a.ll;
       float* row = out + render_out_index(a, c, x, y0 + yl, 0);
-      const bool fin = s.yfin[cy] != 0;
-      const float* iv = s.ival + cy * a.ll;
-      for (int z = lane; z < a.zz; z += 32) {
-        const int o = s.owner[c * a.zz + z];
-        row[z] = !fin ? 0.f : o >= 0 ? iv[o] : render_cut_value(a, s, c, yl, z);
+      if (s.yfin[cy]) {
+        const float* iv = s.ival + cy * a.ll;
+        for (int z = lane; z < a.zz; z += 32) {
+          const int o = s.owner[c * a.zz + z];
+          if (o >= 0) row[z] = iv[o];
+        }
+      } else {
+        for (int z = lane; z < a.zz; z += 32)
+          row[z] = render_value(a, s.pos, c, st, z);
       }
     }
 }
 
-// Whether phase 8 has work: a row whose statistics are not all finite, or
-// more interface-cut cells than phase 6 tabulates (out-of-order positions).
-// The same for every thread of the CTA after the barrier that ends phase 5.
-PJZ_HD bool render_needs_full_mix(const RenderSmem& s) {
-  return s.ncut[3] != 0 || s.ncut[0] > kRenderCutCap || s.ncut[1] > kRenderCutCap ||
-         s.ncut[2] > kRenderCutCap;
-}
-
-// Phase 8 (after a barrier, when render_needs_full_mix): the full mix of
-// every cell of rows whose statistics are not all finite, and of the cut
-// cells past the cap in the other rows, over the CTA's threads.
-PJZ_HD void render_phase_full_mix(const RenderArgs& a, const RenderSmem& s, int x,
-                                  int y0, int ny, int tid, int nthr, float* out) {
+// Phase 7 (after a barrier): the interface-cut cells of every row with
+// finite statistics, shared over the CTA's threads (the same few z for
+// every row).
+PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int x,
+                                   int y0, int ny, int tid, int nthr, float* out) {
   for (int c = 0; c < 3; ++c)
-    for (int t = tid; t < ny * a.zz; t += nthr) {
-      const int yl = t / a.zz, z = t - yl * a.zz;
+    for (int t = tid; t < s.ncut[c] * kRenderTileY; t += nthr) {
+      const int yl = t % kRenderTileY, z = s.cut[c * a.zz + t / kRenderTileY];
       const int cy = c * kRenderTileY + yl;
-      const bool far = s.owner[c * a.zz + z] < 0 && s.cutidx[c * a.zz + z] >= kRenderCutCap;
-      if (!s.yfin[cy] || far)
+      if (yl < ny && s.yfin[cy])
         out[render_out_index(a, c, x, y0 + yl, z)] =
             render_value(a, s.pos, c, s.st + cy * a.ll, z);
     }
@@ -623,16 +541,11 @@ __global__ void __launch_bounds__(256, 6) render_epsilon_kernel(const RenderArgs
     render_phase_stage(a, s, l0, ng, x, y0, ny, tid, nthr);
     __syncthreads();
     render_phase_windows(a, s, l0, ng, ny, tid, nthr);
-    if (l0 == 0) render_phase_cut_fractions(a, s, tid, nthr);
   }
-  __syncthreads();
-  render_phase_cut_values(a, s, ny, tid, nthr);
   __syncthreads();
   render_phase_out(a, s, x, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);
-  if (render_needs_full_mix(s)) {  // CTA-uniform
-    __syncthreads();  // placeholders are written before phase 8
-    render_phase_full_mix(a, s, x, y0, ny, tid, nthr, a.out);
-  }
+  __syncthreads();  // placeholders of cut cells are written before phase 7
+  render_phase_cut_cells(a, s, x, y0, ny, tid, nthr, a.out);
 }
 #endif
 

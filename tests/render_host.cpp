@@ -66,17 +66,13 @@ extern "C" int render_host(const float* layers, int ll, int xx, int yy, int zz,
         const int ng = a.group < ll - l0 ? a.group : ll - l0;
         for (int t = 0; t < kThreads; ++t)
           render_phase_stage(a, s, l0, ng, x, y0, ny, t, kThreads);
-        for (int t = 0; t < kThreads; ++t) {
+        for (int t = 0; t < kThreads; ++t)
           render_phase_windows(a, s, l0, ng, ny, t, kThreads);
-          if (l0 == 0) render_phase_cut_fractions(a, s, t, kThreads);
-        }
       }
-      for (int t = 0; t < kThreads; ++t) render_phase_cut_values(a, s, ny, t, kThreads);
       for (int t = 0; t < kThreads; ++t)
         render_phase_out(a, s, x, y0, ny, t >> 5, kThreads >> 5, t & 31, a.out);
-      if (render_needs_full_mix(s))
-        for (int t = 0; t < kThreads; ++t)
-          render_phase_full_mix(a, s, x, y0, ny, t, kThreads, a.out);
+      for (int t = 0; t < kThreads; ++t)
+        render_phase_cut_cells(a, s, x, y0, ny, t, kThreads, a.out);
     }
   for (size_t i = 0; i < kGuard; ++i) {
     uint32_t lo, hi;
