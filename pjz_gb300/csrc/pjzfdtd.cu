@@ -627,7 +627,10 @@ int32_t resolve_seg_x(pjzfdtd_plan* pl) {
   const int slots = sms * per_sm;
   int nseg = std::max(1, slots / tiles_y);
   int seg = (pl->p.xx + nseg - 1) / nseg;
-  seg = std::max(seg, std::min(pl->p.xx, 8));  // keep the halo plane cheap
+  // At least 4 planes per segment: each segment re-reads one halo plane,
+  // and small domains (c0: 128x128x32) need short segments to fill the
+  // SMs at all.
+  seg = std::max(seg, std::min(pl->p.xx, 4));
   pl->seg_x = seg;
   return PJZFDTD_OK;
 }
