@@ -1237,9 +1237,11 @@ int32_t pjzfdtd_batch_create(pjzfdtd_plan* const* plans, int32_t n,
     bt->tt_max = std::max(bt->tt_max, pl->p.tt);
     bt->smem = std::max(bt->smem, pl->smem);
     bt->smem2 = std::max(bt->smem2, pl->smem2);
-    // Segments are at least 8 planes long (or the whole x extent).
+    // Segments are the requested length, else at least 4 planes long (or
+    // the whole x extent; resolve_seg_x).
     const int tiles = (pl->p.yy + pl->tile_y - 1) / pl->tile_y;
-    const int minseg = std::min(pl->p.xx, 8);
+    const int minseg = pl->p.seg_x > 0 ? std::min(pl->p.xx, pl->p.seg_x)
+                                       : std::min(pl->p.xx, 4);
     bt->max_work += tiles * ((pl->p.xx + minseg - 1) / minseg);
   }
   bt->off_args = o;
