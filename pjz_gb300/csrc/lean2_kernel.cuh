@@ -238,11 +238,6 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
   const int ra = item.row;  // buffer row (y = y0 - 2 + ra)
   const int z0 = item.z0;
   const int col = item.col;
-  // Whether this warp holds z-PML quads (warp-uniform): such warps take the
-  // z-PML arithmetic on every lane (state column 0 read where a lane's quad
-  // lies between the slabs) and keep it only on slab lanes, so their lanes
-  // never branch apart.
-  const bool pmlw = __any_sync(0xffffffffu, pml);
   const int y = y0 - 2 + ra;
   const bool in_y = ra < NR && y >= 0 && y < Y;
   const bool do_h1 = in_y;                          // rows 0 .. NR-1
@@ -269,7 +264,7 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
   const float* wave1 = a.wave;
   const float* wave2 = a.snc > 0 ? a.wave + a.snc : nullptr;
   const int ie = ra * Z + z0;   // row ra of every NR-row buffer (and ring A E)
-  const int pi = ra * Pp + (pml ? col : 0);
+  const int pi = ra * Pp + col;
 
   // H update of the quad: E (stride es, rows ra / ra+1, z+1), E of the next
   // plane (E1, or zero), old H (stride hs), PML state comps 0/1 (stride ps).
@@ -292,7 +287,7 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) Q::ld(Ho + c * hs + ie, ho[c]);
-    if (pmlw) {
+    if (pml) {
       Q::ld(Pin + pi, pa);
       Q::ld(Pin + ps + pi, pb);
     }
@@ -303,14 +298,17 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
       const float dEz_y = fsub(ezy[j], ez[j]), dEy_z = fsub(ey1, ey[j]);
       const float dEx_z = fsub(ex1, ex[j]), dEz_x = fsub(e1z[j], ez[j]);
       const float dEy_x = fsub(e1y[j], ey[j]), dEx_y = fsub(exy[j], ex[j]);
-      float zEy = fmul(dEy_z, ikh[j]), zEx = fmul(dEx_z, ikh[j]);
-      if (pmlw) {
+      float zEy, zEx;
+      if (pml) {
         const float na = ffma(ch[j], dEy_z, fmul(bh[j], pa[j]));
         const float nb = ffma(ch[j], dEx_z, fmul(bh[j], pb[j]));
         pa[j] = na;
         pb[j] = nb;
-        zEy = pml ? ffma(dEy_z, ikh[j], na) : zEy;
-        zEx = pml ? ffma(dEx_z, ikh[j], nb) : zEx;
+        zEy = ffma(dEy_z, ikh[j], na);
+        zEx = ffma(dEx_z, ikh[j], nb);
+      } else {
+        zEy = fmul(dEy_z, ikh[j]);
+        zEx = fmul(dEx_z, ikh[j]);
       }
       hn[0][j] = ffma(mdt, fsub(dEz_y, zEy), ho[0][j]);
       hn[1][j] = ffma(mdt, fsub(zEx, dEz_x), ho[1][j]);
@@ -341,7 +339,7 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
       Q::ld(Eo + c * es + ie, eo[c]);
       Q::ld(Cb + c * cs + ie, cb[c]);
     }
-    if (pmlw) {
+    if (pml) {
       Q::ld(Pin + pi, pa);
       Q::ld(Pin + ps + pi, pb);
     }
@@ -352,14 +350,17 @@ __device__ __forceinline__ void lean2_tile(const StreamArgs& sa, int tile, int s
       const float dHz_y = fsub(hz[j], hzm[j]), dHy_z = fsub(hy[j], hy0);
       const float dHx_z = fsub(hx[j], hx0), dHz_x = fsub(hz[j], hzp[j]);
       const float dHy_x = fsub(hy[j], hyp[j]), dHx_y = fsub(hx[j], hxm[j]);
-      float zHy = fmul(dHy_z, ike[j]), zHx = fmul(dHx_z, ike[j]);
-      if (pmlw) {
+      float zHy, zHx;
+      if (pml) {
         const float na = ffma(ce[j], dHy_z, fmul(be[j], pa[j]));
         const float nb = ffma(ce[j], dHx_z, fmul(be[j], pb[j]));
         pa[j] = na;
         pb[j] = nb;
-        zHy = pml ? ffma(dHy_z, ike[j], na) : zHy;
-        zHx = pml ? ffma(dHx_z, ike[j], nb) : zHx;
+        zHy = ffma(dHy_z, ike[j], na);
+        zHx = ffma(dHx_z, ike[j], nb);
+      } else {
+        zHy = fmul(dHy_z, ike[j]);
+        zHx = fmul(dHx_z, ike[j]);
       }
       float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
       if (src) {

@@ -386,12 +386,6 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const int rH = item.row;
   const int z0 = item.z0;
   const int col = item.col;  // z-PML state column of z0 (z-PML quads)
-  // Whether this warp holds z-PML quads (warp-uniform).  Such warps take
-  // the z-PML arithmetic on every lane, reading column 0 of the state where
-  // a lane's quad lies between the slabs, and keep its result only on the
-  // slab lanes (a select), so their lanes never branch apart.
-  const bool pmlw = __any_sync(0xffffffffu, pml);
-  const int colz = pml ? col : 0;
   const bool doH = rH < RH && y0 - 1 + rH >= 0 && y0 - 1 + rH < Y;
   const int yE = y0 + rH;
   const bool doE = rH < TY && yE < Y;
@@ -427,8 +421,8 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
   const int ieH = rH * Z + z0;        // H-phase row rH, E rows rH / rH + 1
   const int ihE = (rH + 1) * Z + z0;  // E-phase buffer row rH + 1
   const int icE = rH * Z + z0;        // coefficient / staging row rH
-  const int pH = rH * Pp + colz;
-  const int pE = (rH + 1) * Pp + colz;
+  const int pH = rH * Pp + col;
+  const int pE = (rH + 1) * Pp + col;
 
   // H^{n+1/2} of the quad at buffer row rH (y = y0 - 1 + rH) of the plane in
   // ring slot `sl` (E of the next plane in slot `sl1`, or zero), into hcur /
@@ -459,7 +453,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       for (int c = 0; c < 3; ++c) Q::ld(Hs + c * RHZ + ieH, ho[c]);
       float pa[4], pb[4], ikh[4], bh[4], ch[4];
       zload(3, ikh);
-      if (pmlw) {
+      if (pml) {
         Q::ld(Ps + pH, pa);
         Q::ld(Ps + RH * Pp + pH, pb);
         zload(4, bh);
@@ -473,14 +467,17 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dEz_y = fsub(ezy[j], ez[j]), dEy_z = fsub(ey1, ey[j]);
         const float dEx_z = fsub(ex1, ex[j]), dEz_x = fsub(e1z[j], ez[j]);
         const float dEy_x = fsub(e1y[j], ey[j]), dEx_y = fsub(exy[j], ex[j]);
-        float zEy = fmul(dEy_z, ikh[j]), zEx = fmul(dEx_z, ikh[j]);
-        if (pmlw) {
+        float zEy, zEx;
+        if (pml) {
           const float na = ffma(ch[j], dEy_z, fmul(bh[j], pa[j]));
           const float nb = ffma(ch[j], dEx_z, fmul(bh[j], pb[j]));
           pa[j] = na;
           pb[j] = nb;
-          zEy = pml ? ffma(dEy_z, ikh[j], na) : zEy;
-          zEx = pml ? ffma(dEx_z, ikh[j], nb) : zEx;
+          zEy = ffma(dEy_z, ikh[j], na);
+          zEx = ffma(dEx_z, ikh[j], nb);
+        } else {
+          zEy = fmul(dEy_z, ikh[j]);
+          zEx = fmul(dEx_z, ikh[j]);
         }
         hx[j] = ffma(mdt, fsub(dEz_y, zEy), ho[0][j]);
         hy[j] = ffma(mdt, fsub(zEx, dEz_x), ho[1][j]);
@@ -525,7 +522,7 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
       const float sig[3] = {Ms[rH], Ms[g.MT + rH], Ms[2 * g.MT + rH]};
       float pa[4], pb[4], ike[4], be[4], ce[4];
       zload(0, ike);
-      if (pmlw) {
+      if (pml) {
         Q::ld(Ps + 2 * RH * Pp + pE, pa);
         Q::ld(Ps + 3 * RH * Pp + pE, pb);
         zload(1, be);
@@ -540,14 +537,17 @@ __device__ __forceinline__ void lean_tile(const StreamArgs& sa, int tile, int se
         const float dHz_y = fsub(hz[j], hzm[j]), dHy_z = fsub(hy[j], hy0);
         const float dHx_z = fsub(hx[j], hx0), dHz_x = fsub(hz[j], hzp[j]);
         const float dHy_x = fsub(hy[j], hyp[j]), dHx_y = fsub(hx[j], hxm[j]);
-        float zHy = fmul(dHy_z, ike[j]), zHx = fmul(dHx_z, ike[j]);
-        if (pmlw) {
+        float zHy, zHx;
+        if (pml) {
           const float na = ffma(ce[j], dHy_z, fmul(be[j], pa[j]));
           const float nb = ffma(ce[j], dHx_z, fmul(be[j], pb[j]));
           pa[j] = na;
           pb[j] = nb;
-          zHy = pml ? ffma(dHy_z, ike[j], na) : zHy;
-          zHx = pml ? ffma(dHx_z, ike[j], nb) : zHx;
+          zHy = ffma(dHy_z, ike[j], na);
+          zHx = ffma(dHx_z, ike[j], nb);
+        } else {
+          zHy = fmul(dHy_z, ike[j]);
+          zHx = fmul(dHx_z, ike[j]);
         }
         float cur[3] = {fsub(dHz_y, zHy), fsub(zHx, dHz_x), fsub(dHy_x, dHx_y)};
         if (src) {
