@@ -1470,27 +1470,30 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
                 xx, yy, zz, magnification);
   if (ll > 1 && !interface_positions)
     return fail(PJZFDTD_ERR_INVALID, "%d interface positions needed", ll - 1);
-  // Layers staged together: all of them while the CTA stays within 48 KB
-  // of shared memory (several CTAs per SM), else fewer, down to one; the
-  // patches' flat indices must keep t * columns below 2^32 (render_div).
-  const int prow = render_patch_rows(magnification);
+  // x cells per CTA (their patches share 1 - 1/(3 nxb) of their rows) and
+  // layers staged together: as many as keep the CTA within 48 KB of shared
+  // memory (several CTAs per SM), trading x cells first; the patches' flat
+  // indices must keep t * columns below 2^32 (render_div).
   const int pcol = render_patch_cols(magnification);
-  auto bytes = [&](int g) {
-    return render_smem_floats(ll, zz, magnification, g) * sizeof(float);
+  auto bytes = [&](int g, int nxb) {
+    return render_smem_floats(ll, zz, magnification, g, nxb) * sizeof(float);
   };
-  auto exact = [&](int g) {
-    return (uint64_t)g * prow * pcol * (uint64_t)pcol < ((uint64_t)1 << 32);
+  auto exact = [&](int g, int nxb) {
+    return (uint64_t)g * render_patch_rows(magnification, nxb) * pcol * (uint64_t)pcol <
+           ((uint64_t)1 << 32);
   };
-  int group = ll;
-  while (group > 1 && (bytes(group) > 48 * 1024 || !exact(group))) --group;
-  const size_t smem = bytes(group);
+  int nxb = std::min(xx, kRenderMaxXCells), group = ll;
+  while (nxb > 1 && (bytes(1, nxb) > 48 * 1024 || !exact(1, nxb))) --nxb;
+  while (group > 1 && (bytes(group, nxb) > 48 * 1024 || !exact(group, nxb))) --group;
+  const int prow = render_patch_rows(magnification, nxb);
+  const size_t smem = bytes(group, nxb);
   const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
   const bool zq_exact =
       (uint64_t)kRenderTileY * (zz / 4) * (uint64_t)(zz / 4) < ((uint64_t)1 << 32);
   const bool layer_fits =  // pixel offsets within a layer are 32-bit
       (uint64_t)(2 * magnification) * xx * (uint64_t)(2 * magnification) * yy <
       ((uint64_t)1 << 31);
-  if (smem > kSmemMax || !exact(group) || !zq_exact || !layer_fits ||
+  if (smem > kSmemMax || !exact(group, nxb) || !zq_exact || !layer_fits ||
       yblocks > 65535)
     return fail(PJZFDTD_ERR_INVALID,
                 "zz = %d with %d layers at magnification %d (or yy = %d) "
@@ -1505,6 +1508,7 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   a.m = magnification;
   a.simple = use_simple_averaging != 0;
   a.group = group;
+  a.nxb = nxb;
   a.sorted = 1;  // nondecreasing without NaN: owners by comparison
   for (int i = 0; i + 1 < ll; ++i)
     if (interface_positions[i] != interface_positions[i] ||
@@ -1518,7 +1522,7 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
   if (smem > 48 * 1024)
     CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
-  const dim3 grid((unsigned)xx, (unsigned)yblocks);
+  const dim3 grid((unsigned)((xx + nxb - 1) / nxb), (unsigned)yblocks);
   k<<<grid, 256, smem, static_cast<cudaStream_t>(stream)>>>(a);
   CUDA_TRY(cudaGetLastError());
   return PJZFDTD_OK;

@@ -56,12 +56,14 @@ namespace pjzfdtd {
 
 constexpr int kRenderMaxLayers = 16;
 constexpr int kRenderTileY = 32;
+constexpr int kRenderMaxXCells = 4;  // x cells per CTA at most
 
 struct RenderArgs {
   const float* layers;  // (ll, 2m*xx, 2m*yy)
   float* out;           // (3, xx, yy, zz)
   int ll, xx, yy, zz, m, simple;
   int group;            // layers staged together (1 .. ll)
+  int nxb;              // x cells per CTA (their patches share rows)
   int sorted;           // positions nondecreasing and free of NaN
   uint32_t col_magic;   // render_col_magic(patch columns)
   uint32_t row_magic;   // render_col_magic(patch rows)
@@ -90,10 +92,11 @@ PJZ_HD float render_load(const float* layer, size_t i) { return layer[i]; }
 
 PJZ_HD int render_imax(int a, int b) { return a > b ? a : b; }
 
-// Pixel patch of one CTA and layer: rows k*x - m .. k*x + 2m - 1 and
-// columns k*y0 - m .. k*(y0 + ny) - 1 (k = 2m), negative indices repeating
-// the edge pixel.
-PJZ_HD int render_patch_rows(int m) { return 3 * m; }
+// Pixel patch of one CTA and layer: for x cells x0 .. x0 + nx - 1, rows
+// k*x0 - m .. k*(x0 + nx) - 1 and columns k*y0 - m .. k*(y0 + ny) - 1 (k =
+// 2m), negative indices repeating the edge pixel; cell x0 + i reads rows
+// k*i .. k*i + 3m - 1 of it.
+PJZ_HD int render_patch_rows(int m, int nx) { return 2 * m * nx + m; }
 PJZ_HD int render_patch_cols(int m) { return 2 * m * kRenderTileY + m; }
 
 // t / d for the patches' flat indices: floor(t * ceil(2^32 / d) / 2^32)
@@ -119,21 +122,21 @@ PJZ_HD int render_div(int t, uint32_t magic) {
 // the pixel offsets u [2m], the interface positions [kRenderMaxLayers], and
 // per component the z cells an interface cuts [3][zz] (int) and their
 // count [4] (int).
-PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group) {
-  return 3 * (size_t)zz + 15 * (size_t)kRenderTileY * ll +
-         3 * kRenderTileY +
-         2 * (size_t)group * render_patch_rows(m) * render_patch_cols(m) + 2 * m +
-         kRenderMaxLayers + 3 * (size_t)zz + 4;
+PJZ_HD size_t render_smem_floats(int ll, int zz, int m, int group, int nxb) {
+  return 3 * (size_t)zz + 15 * (size_t)nxb * kRenderTileY * ll +
+         3 * (size_t)nxb * kRenderTileY +
+         2 * (size_t)group * render_patch_rows(m, nxb) * render_patch_cols(m) +
+         2 * m + kRenderMaxLayers + 3 * (size_t)zz + 4;
 }
 
 // The regions of one CTA's shared memory (render_smem_floats floats).
 struct RenderSmem {
   int* owner;       // [3][zz]
-  WindowStats* st;  // [3][kRenderTileY][ll]
-  float* ival;      // [3][kRenderTileY][ll]
-  int* yfin;        // [3][kRenderTileY]
-  float* pf;        // [group][3m][pc]
-  float* pinv;      // [group][3m][pc]
+  WindowStats* st;  // [nxb][3][kRenderTileY][ll]
+  float* ival;      // [nxb][3][kRenderTileY][ll]
+  int* yfin;        // [nxb][3][kRenderTileY]
+  float* pf;        // [group][2m*nxb + m][pc]
+  float* pinv;      // [group][2m*nxb + m][pc]
   float* u;         // [2m]
   float* pos;       // [kRenderMaxLayers]
   int* cut;         // [3][zz]: z cells no single layer fills
@@ -141,15 +144,16 @@ struct RenderSmem {
   float* end;
 };
 
-PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m, int group) {
-  const int TL = kRenderTileY * ll;
-  const int np = group * render_patch_rows(m) * render_patch_cols(m);
+PJZ_HD RenderSmem render_carve(float* sm, int ll, int zz, int m, int group,
+                              int nxb) {
+  const int TL = nxb * kRenderTileY * ll;
+  const int np = group * render_patch_rows(m, nxb) * render_patch_cols(m);
   RenderSmem s;
   s.owner = reinterpret_cast<int*>(sm);
   s.st = reinterpret_cast<WindowStats*>(s.owner + 3 * zz);
   s.ival = reinterpret_cast<float*>(s.st + 3 * TL);
   s.yfin = reinterpret_cast<int*>(s.ival + 3 * TL);
-  s.pf = reinterpret_cast<float*>(s.yfin + 3 * kRenderTileY);
+  s.pf = reinterpret_cast<float*>(s.yfin + 3 * nxb * kRenderTileY);
   s.pinv = s.pf + np;
   s.u = s.pinv + np;
   s.pos = s.u + 2 * m;
@@ -344,7 +348,7 @@ PJZ_HD void render_phase_setup(const RenderArgs& a, const RenderSmem& s, int tid
     s.pos[kRenderMaxLayers - 1] = 0.f;
   }
   for (int t = tid; t < 2 * a.m; t += nthr) s.u[t] = render_u(a, t);
-  for (int t = tid; t < 3 * kRenderTileY; t += nthr) s.yfin[t] = 1;
+  for (int t = tid; t < 3 * a.nxb * kRenderTileY; t += nthr) s.yfin[t] = 1;
 }
 
 // Phase 2 (after the positions are in shared memory): the filling layer of
@@ -399,9 +403,12 @@ inline void render_phase_cuts(const RenderArgs& a, const RenderSmem& s, int tid,
 constexpr int kRenderStageBatch = 8;
 
 PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
-                               int ng, int x, int y0, int ny, int tid, int nthr) {
+                               int ng, int x0, int nx, int y0, int ny, int tid,
+                               int nthr) {
   const int k = 2 * a.m, pc = render_patch_cols(a.m);
-  const int cols = k * ny + a.m, rows = ng * render_patch_rows(a.m);
+  const int PR = render_patch_rows(a.m, a.nxb);  // rows per layer's patch
+  const int cols = k * ny + a.m, rows = ng * PR;
+  const int live_rows = render_patch_rows(a.m, nx);
   const int PX = k * a.xx, PY = k * a.yy;
   const int n = rows * pc;
   const float* L0 = a.layers + (size_t)l0 * PX * PY;
@@ -414,10 +421,10 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
       const int gr = render_div(t, a.col_magic);  // (layer, row) of the group
       const int cc = t - gr * pc;
       f[b] = 0.f;
-      if (t < n && cc < cols) {
-        const int g = render_div(gr, a.row_magic);  // layer of the group
-        const int r = gr - g * render_patch_rows(a.m);
-        const int px = render_imax(k * x - a.m + r, 0);
+      const int g = render_div(gr, a.row_magic);  // layer of the group
+      const int r = gr - g * PR;
+      if (t < n && cc < cols && r < live_rows) {
+        const int px = render_imax(k * x0 - a.m + r, 0);
         const int py = render_imax(k * y0 - a.m + cc, 0);
         // One layer holds fewer than 2^31 pixels (checked by the host).
         f[b] = render_load(L0 + (size_t)g * PX * PY, (size_t)(px * PY + py));
@@ -435,22 +442,32 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
   }
 }
 
+// Row of the (x cell, component, y cell) statistics of a CTA.
+PJZ_HD int render_cy(int xi, int c, int yl) { return (3 * xi + c) * kRenderTileY + yl; }
+
 // Phase 5, per group: window statistics and one-layer values of the
-// (component, row, layer) windows of the staged patches.
+// (x cell, layer, component, row) windows of the staged patches.
 PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l0,
-                                 int ng, int ny, int tid, int nthr) {
+                                 int ng, int nx, int ny, int tid, int nthr) {
   const int pc = render_patch_cols(a.m);
-  const int np1 = render_patch_rows(a.m) * pc;  // one layer's patch
-  for (int t = tid; t < 3 * ny * ng; t += nthr) {
-    int g = 0, r = t;
+  const int np1 = render_patch_rows(a.m, a.nxb) * pc;  // one layer's patch
+  const int per = 3 * ny * ng;                         // items per x cell
+  for (int t = tid; t < nx * per; t += nthr) {
+    int xi = 0, r = t;
+    while (r >= per) {  // nx is small: at most a.nxb
+      r -= per;
+      ++xi;
+    }
+    int g = 0;
     while (r >= 3 * ny) {  // ng is small: at most kRenderMaxLayers
       r -= 3 * ny;
       ++g;
     }
     const int c = r >= 2 * ny ? 2 : (r >= ny ? 1 : 0), yl = r - c * ny;
-    const int cy = c * kRenderTileY + yl;
+    const int cy = render_cy(xi, c, yl);
     const int i = cy * a.ll + l0 + g;
-    s.st[i] = render_window(a, c, yl, s.pf + g * np1, s.pinv + g * np1, pc, s.u);
+    const int off = g * np1 + 2 * a.m * xi * pc;  // cell xi's rows of the patch
+    s.st[i] = render_window(a, c, yl, s.pf + off, s.pinv + off, pc, s.u);
     s.ival[i] = render_interior(a, c, s.st[i]);
     if (!render_finite(s.st[i])) s.yfin[cy] = 0;  // any writer stores 0
   }
@@ -463,16 +480,18 @@ PJZ_HD void render_phase_windows(const RenderArgs& a, const RenderSmem& s, int l
 // 16-byte stores.  Otherwise warp `w` takes whole (component, y) rows, lane
 // `lane` along z, skipping cut cells.  A row whose statistics are not all
 // finite takes the full mix at every z here.
-PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
-                             int y0, int ny, int w, int nw, int lane,
+PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x0,
+                             int nx, int y0, int ny, int w, int nw, int lane,
                              float* out) {
   const int tid = w * 32 + lane, nthr = nw * 32;
   if (render_quads(a, out)) {
     const int zq = a.zz >> 2;
+    for (int xi = 0; xi < nx; ++xi)
     for (int c = 0; c < 3; ++c)
       for (int t = tid; t < ny * zq; t += nthr) {
         const int yl = render_div(t, a.zq_magic), z = 4 * (t - yl * zq);
-        const int cy = c * kRenderTileY + yl;
+        const int cy = render_cy(xi, c, yl);
+        const int x = x0 + xi;
         float v[4];
         if (s.yfin[cy]) {
           const float* iv = s.ival + cy * a.ll;
@@ -489,9 +508,11 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
       }
     return;
   }
+  for (int xi = 0; xi < nx; ++xi)
   for (int c = 0; c < 3; ++c)
     for (int yl = w; yl < ny; yl += nw) {
-      const int cy = c * kRenderTileY + yl;
+      const int cy = render_cy(xi, c, yl);
+      const int x = x0 + xi;
       const WindowStats* st = s.st + cy * a.ll;
       float* row = out + render_out_index(a, c, x, y0 + yl, 0);
       if (s.yfin[cy]) {
@@ -510,27 +531,30 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x,
 // Phase 7 (after a barrier): the interface-cut cells of every row with
 // finite statistics, shared over the CTA's threads (the same few z for
 // every row).
-PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int x,
-                                   int y0, int ny, int tid, int nthr, float* out) {
+PJZ_HD void render_phase_cut_cells(const RenderArgs& a, const RenderSmem& s, int x0,
+                                   int nx, int y0, int ny, int tid, int nthr,
+                                   float* out) {
+  for (int xi = 0; xi < nx; ++xi)
   for (int c = 0; c < 3; ++c)
     for (int t = tid; t < s.ncut[c] * kRenderTileY; t += nthr) {
       const int yl = t % kRenderTileY, z = s.cut[c * a.zz + t / kRenderTileY];
-      const int cy = c * kRenderTileY + yl;
+      const int cy = render_cy(xi, c, yl);
       if (yl < ny && s.yfin[cy])
-        out[render_out_index(a, c, x, y0 + yl, z)] =
+        out[render_out_index(a, c, x0 + xi, y0 + yl, z)] =
             render_value(a, s.pos, c, s.st + cy * a.ll, z);
     }
 }
 
 #if defined(__CUDACC__) && defined(PJZ_RENDER_KERNEL)  // kern_render.cu only
-// grid (xx, ceil(yy / kRenderTileY)), a multiple of 32 threads (at least
-// 96); dynamic shared memory render_smem_floats(ll, zz, m, group) floats.
+// grid (ceil(xx / nxb), ceil(yy / kRenderTileY)), a multiple of 32
+// threads (at least 96); dynamic shared memory
+// render_smem_floats(ll, zz, m, group, nxb) floats.
 __global__ void __launch_bounds__(256, 6) render_epsilon_kernel(const RenderArgs a) {
   extern __shared__ __align__(16) float rsm[];
-  const int x = blockIdx.x, y0 = blockIdx.y * kRenderTileY;
-  const int ny = min(kRenderTileY, a.yy - y0);
+  const int x0 = blockIdx.x * a.nxb, y0 = blockIdx.y * kRenderTileY;
+  const int nx = min(a.nxb, a.xx - x0), ny = min(kRenderTileY, a.yy - y0);
   const int tid = threadIdx.x, nthr = blockDim.x;
-  const RenderSmem s = render_carve(rsm, a.ll, a.zz, a.m, a.group);
+  const RenderSmem s = render_carve(rsm, a.ll, a.zz, a.m, a.group, a.nxb);
   render_phase_setup(a, s, tid, nthr);
   __syncthreads();
   render_phase_occupancy(a, s, tid, nthr);
@@ -538,14 +562,14 @@ __global__ void __launch_bounds__(256, 6) render_epsilon_kernel(const RenderArgs
     const int ng = min(a.group, a.ll - l0);
     __syncthreads();  // the previous group's windows are done with the patches
     if (l0 == 0) render_phase_cuts(a, s, tid, nthr);
-    render_phase_stage(a, s, l0, ng, x, y0, ny, tid, nthr);
+    render_phase_stage(a, s, l0, ng, x0, nx, y0, ny, tid, nthr);
     __syncthreads();
-    render_phase_windows(a, s, l0, ng, ny, tid, nthr);
+    render_phase_windows(a, s, l0, ng, nx, ny, tid, nthr);
   }
   __syncthreads();
-  render_phase_out(a, s, x, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);
+  render_phase_out(a, s, x0, nx, y0, ny, tid >> 5, nthr >> 5, tid & 31, a.out);
   __syncthreads();  // placeholders of cut cells are written before phase 7
-  render_phase_cut_cells(a, s, x, y0, ny, tid, nthr, a.out);
+  render_phase_cut_cells(a, s, x0, nx, y0, ny, tid, nthr, a.out);
 }
 #endif
 

@@ -32,14 +32,14 @@ def host(tmp_path_factory):
   h = ctypes.CDLL(lib)
   P = ctypes.c_void_p
   I = ctypes.c_int
-  h.render_host.argtypes = [P, I, I, I, I, I, P, I, I, P]
+  h.render_host.argtypes = [P, I, I, I, I, I, P, I, I, I, P]
   h.render_host.restype = I
   h.render_owner_mismatches.argtypes = [P, I, I, I]
   h.render_owner_mismatches.restype = I
   return h
 
 
-def render(host, layers, pos, m, zz, simple=False, finite=True, group=0):
+def render(host, layers, pos, m, zz, simple=False, finite=True, group=0, nxb=4):
   layers = np.ascontiguousarray(layers, np.float32)
   ll, px, py = layers.shape
   xx, yy = px // (2 * m), py // (2 * m)
@@ -47,7 +47,7 @@ def render(host, layers, pos, m, zz, simple=False, finite=True, group=0):
   out = np.full((3, xx, yy, zz), np.nan, np.float32)
   bad = host.render_host(layers.ctypes.data, ll, xx, yy, zz, m,
                          pos.ctypes.data if pos.size else None, int(simple),
-                         group, out.ctypes.data)
+                         group, nxb, out.ctypes.data)
   assert bad == 0, "a read or write left its array"
   if finite:
     assert np.isfinite(out).all(), "an output was not written"
@@ -90,6 +90,20 @@ def test_owner_by_comparison_matches_exact_fractions(host):
   for pos in cases:
     pos = np.ascontiguousarray(pos, np.float32)
     assert host.render_owner_mismatches(pos.ctypes.data, len(pos) + 1, -3, 16) == 0, pos
+
+
+@pytest.mark.parametrize("xx,nxb", [(7, 1), (7, 2), (7, 3), (9, 4), (1, 4)])
+def test_x_cells_per_cta_give_the_same_floats(host, xx, nxb):
+  """Several x cells per CTA (their patches share rows; the last CTA of a
+  row may hold fewer) change no output bit."""
+  rng = np.random.default_rng(xx * 10 + nxb)
+  m, zz = 2, 10
+  layers = rng.uniform(1.0, 12.25, (3, 2 * m * xx, 2 * m * 35))
+  pos = np.array([2.5, 6.25], np.float32)
+  want = render(host, layers, pos, m, zz, nxb=1)
+  np.testing.assert_array_equal(render(host, layers, pos, m, zz, nxb=nxb), want)
+  np.testing.assert_array_equal(render(host, layers, pos, m, zz, nxb=nxb, group=1),
+                                want)
 
 
 @pytest.mark.parametrize("ll,m", [(5, 2), (16, 1), (3, 3)])
