@@ -1470,10 +1470,10 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
                 xx, yy, zz, magnification);
   if (ll > 1 && !interface_positions)
     return fail(PJZFDTD_ERR_INVALID, "%d interface positions needed", ll - 1);
-  // x cells per CTA (their patches share 1 - 1/(3 nxb) of their rows) and
-  // layers staged together: as many as keep the CTA within 48 KB of shared
-  // memory (several CTAs per SM), trading x cells first; the patches' flat
-  // indices must keep t * columns below 2^32 (render_div).
+  // x cells per CTA (their patches share rows) and layers staged together:
+  // as many as keep the CTA within 36 KB of shared memory (six CTAs per
+  // SM), trading x cells first; the patches' flat indices must keep
+  // t * columns below 2^32 (render_div).
   const int pcol = render_patch_cols(magnification);
   auto bytes = [&](int g, int nxb) {
     return render_smem_floats(ll, zz, magnification, g, nxb) * sizeof(float);
@@ -1483,8 +1483,9 @@ int32_t pjzfdtd_render_epsilon(const float* layers, int32_t ll, int32_t xx,
            ((uint64_t)1 << 32);
   };
   int nxb = std::min(xx, kRenderMaxXCells), group = ll;
-  while (nxb > 1 && (bytes(1, nxb) > 48 * 1024 || !exact(1, nxb))) --nxb;
-  while (group > 1 && (bytes(group, nxb) > 48 * 1024 || !exact(group, nxb))) --group;
+  constexpr size_t kBudget = 36 * 1024;
+  while (nxb > 1 && (bytes(1, nxb) > kBudget || !exact(1, nxb))) --nxb;
+  while (group > 1 && (bytes(group, nxb) > kBudget || !exact(group, nxb))) --group;
   const int prow = render_patch_rows(magnification, nxb);
   const size_t smem = bytes(group, nxb);
   const long long yblocks = ((long long)yy + kRenderTileY - 1) / kRenderTileY;
