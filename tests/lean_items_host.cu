@@ -19,3 +19,21 @@ extern "C" int lean_items_host(int Z, int rows, int plo, int phi, int esz,
   }
   return n;
 }
+
+// LeanGeom<T> of a (tile_y, zz, z-PML width) shape: byte offsets e, h, c,
+// m, p and the slot size, then the new-H, new-E and new-PML-state sizes.
+extern "C" void lean_geom_host(int ty, int z, int p, int esz, long long* out) {
+  if (esz == 2) {
+    const LeanGeom<__half> g(ty, z, p);
+    const long long v[] = {g.e_off, g.h_off, g.c_off, g.m_off, g.p_off, g.stage,
+                           (long long)g.hn_bytes(), (long long)g.en_bytes(),
+                           (long long)g.pn_bytes(), g.Pp};
+    for (int i = 0; i < 10; ++i) out[i] = v[i];
+  } else {
+    const LeanGeom<float> g(ty, z, p);
+    const long long v[] = {g.e_off, g.h_off, g.c_off, g.m_off, g.p_off, g.stage,
+                           (long long)g.hn_bytes(), (long long)g.en_bytes(),
+                           (long long)g.pn_bytes(), g.Pp};
+    for (int i = 0; i < 10; ++i) out[i] = v[i];
+  }
+}

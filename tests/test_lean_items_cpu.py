@@ -12,7 +12,7 @@ import subprocess
 import numpy as np
 import pytest
 
-from test_smem_model_cpu import lean_items
+from test_smem_model_cpu import lean_geom, lean_items
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
@@ -33,6 +33,8 @@ def lib(tmp_path_factory):
   I, P = ctypes.c_int, ctypes.c_void_p
   h.lean_items_host.argtypes = [I, I, I, I, I, P, P, P, P, I]
   h.lean_items_host.restype = I
+  h.lean_geom_host.argtypes = [I, I, I, I, P]
+  h.lean_geom_host.restype = None
   return h
 
 
@@ -57,3 +59,17 @@ def test_model_items_are_the_kernel_items(lib, esz, Z, TY, plo, phi):
     np.testing.assert_array_equal(buf[1][:n], z0[order])
     np.testing.assert_array_equal(buf[2][:n], col[order])
     np.testing.assert_array_equal(buf[3][:n].astype(bool), pml[order])
+
+
+@pytest.mark.parametrize("esz", [4, 2])
+@pytest.mark.parametrize("Z,TY", [(64, 14), (64, 28), (48, 19), (32, 29), (32, 28)])
+@pytest.mark.parametrize("P", [0, 8, 12, 16, 24])
+def test_model_geometry_is_the_kernel_geometry(lib, esz, Z, TY, P):
+  """The byte layout the alignment tests check (``lean_geom``) is the
+  kernels' ``LeanGeom``."""
+  out = np.zeros(10, np.int64)
+  lib.lean_geom_host(TY, Z, P, esz, out.ctypes.data)
+  g = lean_geom(TY, Z, P, esz)
+  want = [g["e"], g["h"], g["c"], g["m"], g["p"], g["stage"], g["hn"], g["en"],
+          g["pn"], g["Pp"]]
+  assert out.tolist() == want
