@@ -6,6 +6,8 @@ Public API (mirrors pjz's ``src/pjz/_field.py``):
   * :func:`fdtdz` -- drop-in for the ``fdtdz_jax.fdtdz`` engine call;
   * :func:`epsilon` -- pjz's Yee-cell permittivity rendering
     (``src/pjz/_epsilon.py``) on the GPU;
+  * :func:`field_voxel_jvp` -- forward-mode derivatives of ``field`` with
+    respect to single permittivity voxels (tangent-linear solves);
   * :class:`engine.Plan` -- the plan/run API over the C ABI.
 """
 
@@ -13,7 +15,8 @@ from ._field import SimParams, field
 from ._fdtdz import LaunchParams, fdtdz
 from ._scatter import scatter
 from ._epsilon import epsilon
+from ._tangent import field_voxel_jvp
 from . import engine
 
 __all__ = ["SimParams", "field", "scatter", "fdtdz", "LaunchParams", "epsilon",
-           "engine"]
+           "field_voxel_jvp", "engine"]
