@@ -48,8 +48,10 @@
 
 #ifdef __CUDACC__
 #define PJZ_HD __host__ __device__ __forceinline__
+#define PJZ_UNROLL _Pragma("unroll")
 #else
 #define PJZ_HD inline
+#define PJZ_UNROLL
 #endif
 
 namespace pjzfdtd {
@@ -207,12 +209,12 @@ PJZ_HD WindowStats render_window_m(const RenderArgs& a, int c, int yl,
   const int ioff = c == 0 ? m : 0;           // rows shifted unless Ex
   const int joff = k * yl + (c == 1 ? m : 0);  // columns shifted unless Ey
   float s = 0.f, si = 0.f, sxu = 0.f, syu = 0.f;
-#pragma unroll
+PJZ_UNROLL
   for (int i = 0; i < k; ++i) {
     const float ui = u[i];
     const float* rf = pf + (i + ioff) * pc + joff;
     const float* ri = pinv + (i + ioff) * pc + joff;
-#pragma unroll
+PJZ_UNROLL
     for (int j = 0; j < k; ++j) {
       const float f = rf[j];
       s += f;
@@ -344,7 +346,7 @@ PJZ_HD void render_store4(float* p, const float v[4]) {
 PJZ_HD void render_phase_setup(const RenderArgs& a, const RenderSmem& s, int tid,
                                int nthr) {
   if (tid == 0) {  // constant indices: the arguments stay in parameter space
-#pragma unroll
+PJZ_UNROLL
     for (int i = 0; i < kRenderMaxLayers - 1; ++i)
       s.pos[i] = i < a.ll - 1 ? a.pos[i] : 0.f;
     s.pos[kRenderMaxLayers - 1] = 0.f;
@@ -417,7 +419,7 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
   for (int t0 = tid; t0 < n; t0 += kRenderStageBatch * nthr) {
     float f[kRenderStageBatch];
     unsigned live = 0;  // bit b: pixel t0 + b * nthr is staged
-#pragma unroll
+PJZ_UNROLL
     for (int b = 0; b < kRenderStageBatch; ++b) {
       const int t = t0 + b * nthr;
       const int gr = render_div(t, a.col_magic);  // (layer, row) of the group
@@ -433,7 +435,7 @@ PJZ_HD void render_phase_stage(const RenderArgs& a, const RenderSmem& s, int l0,
         live |= 1u << b;
       }
     }
-#pragma unroll
+PJZ_UNROLL
     for (int b = 0; b < kRenderStageBatch; ++b) {
       const int t = t0 + b * nthr;
       if (live >> b & 1u) {
@@ -499,10 +501,10 @@ PJZ_HD void render_phase_out(const RenderArgs& a, const RenderSmem& s, int x0,
           const float* iv = s.ival + cy * a.ll;
           int o[4];
           render_owner4(s.owner + c * a.zz + z, o);
-#pragma unroll
+PJZ_UNROLL
           for (int j = 0; j < 4; ++j) v[j] = o[j] >= 0 ? iv[o[j]] : 0.f;
         } else {
-#pragma unroll
+PJZ_UNROLL
           for (int j = 0; j < 4; ++j)
             v[j] = render_value(a, s.pos, c, s.st + cy * a.ll, z + j);
         }
